@@ -1,0 +1,153 @@
+/*
+ * pfgpu.h - C ABI of the GB300 (sm_103a) phase-field step library libpfgpu.so
+ *
+ * Drop-in replacement for the time step of the reference program var_diff.x
+ * (smjim/phase-field-microstructure-evolution):
+ *   - the loop body src/var_diff.f90:474-1118 (14 timed phases + statistics),
+ *   - the FFT wrappers src/f_trans.f90:1-15 and src/inv_trans.f90:1-13,
+ *   - the wavenumber tables src/k_space.f90:4-67.
+ * The reference calls these as implicit-interface Fortran externals with
+ * everything passed by reference (src/var_diff.f90:565,635,869-870,944,964,
+ * 994,1003-1008,1045 and :466); this header offers
+ *   (1) a step-level API (pf_create / pf_set_fields / pf_step / pf_get_fields /
+ *       pf_destroy) that replaces the whole loop body on one GPU, and
+ *   (2) compatibility shims with the exact Fortran signatures of f_trans,
+ *       inv_trans and k_space for a single-rank (ist = 1, ien = N) layout.
+ * Plain pointers and sizes only; every call returns 0 on success and a
+ * negative PF_E* code on failure, with a message from pf_last_error().
+ * Host arrays belong to the caller; device buffers belong to the run.
+ */
+#ifndef PFGPU_H
+#define PFGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PFGPU_ABI_VERSION 1
+
+/* status codes */
+#define PF_OK 0
+#define PF_EINVAL (-1)     /* bad argument / unsupported size */
+#define PF_ECUDA (-2)      /* CUDA runtime error (message has details) */
+#define PF_ENOMEM (-3)     /* device allocation failed */
+#define PF_ENONFINITE (-4) /* a step produced NaN/Inf (fields left as computed) */
+#define PF_EIO (-5)        /* file I/O error */
+
+/* mobility forms of the concentration equation */
+#define PF_MOB_REFERENCE 0 /* mob = D_L + 2(1 - sum phi_i^2) D_gb  (src/var_diff.f90:893-898) */
+#define PF_MOB_C1MC 1      /* mob = D_L (1 + c (1 - c)) */
+
+/* arithmetic of the step */
+#define PF_FP32_FUSED 32 /* fused sm_103a kernels, FP32 fields and FFTs */
+#define PF_FP64_PLAIN 64 /* plain FP64 path: cuFFT + one kernel per reference phase */
+
+/* Coefficients of one run; names and meaning follow input.txt
+ * (src/var_diff.f90:104-121). dx, dy, dz are not used by the reference step. */
+typedef struct pf_config {
+  int nx, ny, nz;        /* Nx, Ny, Nz */
+  int var;               /* number of order parameters (last one = precipitate) */
+  double t_step;         /* dt */
+  double grad_coeff_phi; /* kappa_phi */
+  double grad_coeff_c;   /* kappa_c */
+  double D_S;            /* read but unused by the reference step */
+  double D_L;            /* bulk mobility, also D_mean (src/var_diff.f90:916) */
+  double D_gb;           /* grain-boundary mobility */
+  double mob_phi;        /* Allen-Cahn mobility L */
+  double sigma_1, sigma_2;
+  double am, ap, con_0_mat, con_0_ppt;
+  int mobility;          /* PF_MOB_* */
+  int precision;         /* PF_FP32_FUSED or PF_FP64_PLAIN */
+  int device;            /* CUDA device ordinal */
+  int reserved[5];
+} pf_config;
+
+/* Diagnostics of one step.  f_int, f_eta, f_ch and the statistics c_min,
+ * c_max, phi_min (min over cells of sum_i phi_i^2) and phi_P_max describe the
+ * fields at the START of the step: exactly the values that var_diff.f90
+ * writes to summary.dat for that step (:1058-1074, statistics lagged by one
+ * step, :1076-1118).  mass = sum_cells c at the start of the step. */
+typedef struct pf_diag {
+  int step; /* 1-based step number since pf_create / the last pf_set_fields */
+  int nonfinite;
+  double f_int, f_eta, f_ch, e_tot;
+  double c_max, c_min, phi_min, phi_P_max;
+  double mass;
+} pf_diag;
+
+typedef struct pf_run pf_run;
+
+/* ---- step-level API (replaces src/var_diff.f90:474-1118) ---------------- */
+
+/* Create a run on cfg->device: validates the sizes, allocates the resident
+ * state and builds the FP64 wavenumber/twiddle tables.  Supported grids:
+ * Nx, Ny, Nz in {16, 32, 64, 128, 256} (FP32 path; every (Ny, Nz) pair with
+ * Ny == Nz plus the non-cubic pairs listed by pf_supported_shape), 1 <= var
+ * <= 48. */
+int pf_create(const pf_config* cfg, pf_run** out);
+
+/* 1 if (nx, ny, nz, var) can run on the given precision path, else 0. */
+int pf_supported_shape(int nx, int ny, int nz, int var, int precision);
+
+/* Upload fields from host arrays in Fortran order: phi(var, x, y, z) with var
+ * fastest (src/var_diff.f90:154) and con(x, y, z) (:143), REAL*8. Resets the
+ * step counter. */
+int pf_set_fields(pf_run* run, const double* phi_aos, const double* con);
+
+/* Advance nsteps steps.  diag (may be NULL) receives nsteps records. Returns
+ * PF_ENONFINITE if any step produced a non-finite value. */
+int pf_step(pf_run* run, int nsteps, pf_diag* diag);
+
+/* Download fields into host arrays in the pf_set_fields layout. */
+int pf_get_fields(pf_run* run, double* phi_aos, double* con);
+
+/* Release device memory and the run. */
+int pf_destroy(pf_run* run);
+
+/* Last error message of the calling thread ("" if none). */
+const char* pf_last_error(void);
+
+/* ---- batched API: many same-shape runs advanced by one set of launches --- */
+typedef struct pf_batch pf_batch;
+int pf_batch_create(const pf_config* cfgs, int nruns, pf_batch** out);
+int pf_batch_set_fields(pf_batch* b, int run, const double* phi_aos, const double* con);
+/* diag (may be NULL) receives nruns * nsteps records, run-major. */
+int pf_batch_step(pf_batch* b, int nsteps, pf_diag* diag);
+int pf_batch_get_fields(pf_batch* b, int run, double* phi_aos, double* con);
+int pf_batch_destroy(pf_batch* b);
+
+/* ---- Fortran compatibility shims (single rank, FP64, whole grid) ---------
+ * Same argument lists as the reference subroutines, all by reference, with
+ * gfortran/ifort-on-Linux name mangling.  ist = (1,1,1), ien = (Nx,Ny,Nz);
+ * the complex array uses P3DFFT's transposed (STRIDE1) order with
+ * fst = (1,1,1), fen = (Nz, Ny, Nx/2+1): dimension 1 = z, 2 = y, 3 = kx.
+ * They run on the FP64 GPU path (device 0 unless pf_shim_device is called).
+ */
+/* f_trans.f90:1   subroutine f_trans(in, out, Nx, Ny, Nz, ist, ien, fst, fen) */
+void f_trans_(const double* in, double* out_cplx, const int* Nx, const int* Ny, const int* Nz,
+              const int* ist, const int* ien, const int* fst, const int* fen);
+/* inv_trans.f90:1 subroutine inv_trans(in, out, ist, ien, fst, fen) */
+void inv_trans_(const double* in_cplx, double* out, const int* ist, const int* ien, const int* fst,
+                const int* fen);
+/* k_space.f90:4   subroutine k_space(Nx, Ny, Nz, fst, fen, kf, kf_sq, kf_4) */
+void k_space_(const int* Nx, const int* Ny, const int* Nz, const int* fst, const int* fen, double* kf,
+              double* kf_sq, double* kf_4);
+/* select the device used by the shims; returns PF_OK or an error code */
+int pf_shim_device(int device);
+
+/* ---- host-side helpers of the drop-in driver (no GPU needed) ------------- */
+
+/* The reference's RNG ran_2 (src/ran_2.f90:1-40) with its saved state kept in
+ * *state (an opaque 40-int buffer zeroed by pf_ran2_init). */
+typedef struct pf_ran2_state {
+  int idum2, iy, iv[32];
+  int initialised;
+  int pad[5];
+} pf_ran2_state;
+void pf_ran2_init(pf_ran2_state* st);
+double pf_ran2(pf_ran2_state* st, int* idum);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PFGPU_H */

@@ -1,0 +1,17 @@
+"""GB300-native semi-implicit spectral phase-field step (drop-in for the time
+step of var_diff.x from smjim/phase-field-microstructure-evolution).
+
+The compute path is the CUDA library ``libpfgpu.so`` (``csrc/``, C ABI in
+``include/pfgpu.h``); this package holds its build recipe, the ctypes binding
+and the host-side mirror of the reference's input/output files.  There is no
+CPU fallback: every entry point fails loudly when the library or a GPU is
+missing.
+"""
+from . import build as build_mod
+from .pfgpu import (Batch, Config, Diag, PFError, Ran2, Run, load_library, library_path, make_config,
+                    PF_FP32_FUSED, PF_FP64_PLAIN, PF_MOB_C1MC, PF_MOB_REFERENCE, EXPORTED)
+
+
+def build(force: bool = False, verbose: bool = False):
+    """Compile libpfgpu.so for sm_103a (in-tree, ``_build/``)."""
+    return build_mod.build(force=force, verbose=verbose)

@@ -1,0 +1,631 @@
+// C ABI of libpfgpu.so (include/pfgpu.h): run/batch management, FP64 table
+// construction, CUDA-graph step driver and host<->device field transfer for
+// the fused FP32 path.  The FP64 plain path and the Fortran shims live in
+// pf_plain64.cu, the host-side RNG in pf_host.cpp.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/pfgpu.h"
+#include "pf_internal.h"
+#include "pf_plain64.h"
+
+namespace pf {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+static int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define PF_CUDA(call)                                                                            \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) return fail(PF_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                       __FILE__, __LINE__);                                      \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Per-step reduction of block partials into one diagnostic record.
+// One block per run, fixed summation order: results do not depend on how many
+// other runs share the launch.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) reduce_diag_kernel(const RunParams* __restrict__ runs, const Shape sh) {
+  const RunParams& rp = runs[blockIdx.x];
+  __shared__ double sd[5][256];
+  __shared__ float sf[4][256];
+  const int t = threadIdx.x;
+  double a_eta = 0, a_ch = 0, a_mass = 0, a_int = 0, a_bad = 0;
+  float cmin = 1.f, cmax = 0.f, pmin = 1.f, ppmax = 0.f;
+  const int nb = sh.nblk_x;
+  for (int i = t; i < nb; i += blockDim.x) {
+    a_eta += rp.part_x[XD_FETA * nb + i];
+    a_ch += rp.part_x[XD_FCH * nb + i];
+    a_mass += rp.part_x[XD_MASS * nb + i];
+    cmin = fminf(cmin, (float)rp.part_x[XD_CMIN * nb + i]);
+    cmax = fmaxf(cmax, (float)rp.part_x[XD_CMAX * nb + i]);
+    pmin = fminf(pmin, (float)rp.part_x[XD_PHIMIN * nb + i]);
+    ppmax = fmaxf(ppmax, (float)rp.part_x[XD_PHIPMAX * nb + i]);
+    a_bad += rp.part_x[XD_NONFINITE * nb + i];
+  }
+  for (int i = t; i < sh.nblk_yz; i += blockDim.x) a_int += rp.part_yz[i];
+  sd[0][t] = a_eta; sd[1][t] = a_ch; sd[2][t] = a_mass; sd[3][t] = a_int; sd[4][t] = a_bad;
+  sf[0][t] = cmin; sf[1][t] = cmax; sf[2][t] = pmin; sf[3][t] = ppmax;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (t < s) {
+#pragma unroll
+      for (int q = 0; q < 5; ++q) sd[q][t] += sd[q][t + s];
+      sf[0][t] = fminf(sf[0][t], sf[0][t + s]);
+      sf[1][t] = fmaxf(sf[1][t], sf[1][t + s]);
+      sf[2][t] = fminf(sf[2][t], sf[2][t + s]);
+      sf[3][t] = fmaxf(sf[3][t], sf[3][t + s]);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    const int step = *rp.counter;
+    double* d = rp.diag + (size_t)(step % rp.ring) * DR_COUNT;
+    d[DR_STEP] = step + 1;
+    d[DR_FINT] = sd[3][0];
+    d[DR_FETA] = sd[0][0];
+    d[DR_FCH] = sd[1][0];
+    d[DR_CMIN] = sf[0][0];
+    d[DR_CMAX] = sf[1][0];
+    d[DR_PHIMIN] = sf[2][0];
+    d[DR_PHIPMAX] = sf[3][0];
+    d[DR_MASS] = sd[2][0];
+    d[DR_NONFINITE] = sd[4][0];
+    *rp.counter = step + 1;
+  }
+}
+
+// Fortran-order host fields (REAL*8) <-> float SoA staging [f][z][y][x]
+__global__ void aos_to_soa_kernel(const double* __restrict__ phi, const double* __restrict__ con, float* __restrict__ fin,
+                                  int V, size_t ncell) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= ncell) return;
+  for (int f = 0; f < V; ++f) fin[(size_t)f * ncell + i] = (float)phi[i * V + f];
+  fin[(size_t)V * ncell + i] = (float)con[i];
+}
+__global__ void soa_to_aos_kernel(const float* __restrict__ fin, double* __restrict__ phi, double* __restrict__ con,
+                                  int V, size_t ncell) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= ncell) return;
+  for (int f = 0; f < V; ++f) phi[i * V + f] = (double)fin[(size_t)f * ncell + i];
+  con[i] = (double)fin[(size_t)V * ncell + i];
+}
+
+// ---------------------------------------------------------------------------
+// FP64 tables
+// ---------------------------------------------------------------------------
+static void twiddles(int L, std::vector<float2>& out) {
+  out.resize(L);
+  const double pi = std::atan(1.0) * 4.0;
+  for (int j = 0; j < L; ++j) {
+    // reduce the angle to the first octant for accuracy, then rebuild
+    const double a = 2.0 * pi * (double)j / (double)L;
+    out[j] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
+  }
+}
+
+// src/k_space.f90:13-59: m' = m (m <= n/2) else m - n; q = m' * (2 pi / n);
+// kf = i q but 0 where 2m = n; kf_sq = -q^2; kf_4 = q^4.
+static void axis_tables(int n, int count, std::vector<float>& q2, std::vector<float>& q4, std::vector<float>& qn) {
+  const double pi = std::atan(1.0) * 4.0;
+  const double unit = 2.0 * pi / (double)n;
+  q2.resize(count); q4.resize(count); qn.resize(count);
+  for (int m = 0; m < count; ++m) {
+    const int mp = (m <= n / 2) ? m : m - n;
+    const double q = (double)mp * unit;
+    q2[m] = (float)(q * q);
+    q4[m] = (float)(q * q * q * q);
+    qn[m] = (2 * m == n) ? 0.0f : (float)q;
+  }
+}
+
+struct DevTables {
+  void* base = nullptr;
+  Shape sh;
+};
+
+static int build_tables(int Nx, int Ny, int Nz, DevTables& t) {
+  std::vector<float2> twM, twN, twY, twZ;
+  twiddles(Nx / 2, twM);
+  twiddles(Nx, twN);
+  twiddles(Ny, twY);
+  twiddles(Nz, twZ);
+  std::vector<float> a[9];
+  const int Kx = Nx / 2 + 1;
+  axis_tables(Nx, Kx, a[0], a[3], a[6]);
+  axis_tables(Ny, Ny, a[1], a[4], a[7]);
+  axis_tables(Nz, Nz, a[2], a[5], a[8]);
+  size_t bytes = 0;
+  auto align = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t off_tw[4], off_a[9];
+  const std::vector<float2>* tws[4] = {&twM, &twN, &twY, &twZ};
+  for (int i = 0; i < 4; ++i) { off_tw[i] = bytes; bytes = align(bytes + tws[i]->size() * sizeof(float2)); }
+  for (int i = 0; i < 9; ++i) { off_a[i] = bytes; bytes = align(bytes + a[i].size() * sizeof(float)); }
+  std::vector<char> host(bytes, 0);
+  for (int i = 0; i < 4; ++i) memcpy(host.data() + off_tw[i], tws[i]->data(), tws[i]->size() * sizeof(float2));
+  for (int i = 0; i < 9; ++i) memcpy(host.data() + off_a[i], a[i].data(), a[i].size() * sizeof(float));
+  PF_CUDA(cudaMalloc(&t.base, bytes));
+  PF_CUDA(cudaMemcpy(t.base, host.data(), bytes, cudaMemcpyHostToDevice));
+  char* b = (char*)t.base;
+  Shape& s = t.sh;
+  s.Nx = Nx; s.Ny = Ny; s.Nz = Nz; s.Kx = Kx;
+  s.twM = (const float2*)(b + off_tw[0]);
+  s.twN = (const float2*)(b + off_tw[1]);
+  s.twY = (const float2*)(b + off_tw[2]);
+  s.twZ = (const float2*)(b + off_tw[3]);
+  s.qx2 = (const float*)(b + off_a[0]); s.qy2 = (const float*)(b + off_a[1]); s.qz2 = (const float*)(b + off_a[2]);
+  s.qx4 = (const float*)(b + off_a[3]); s.qy4 = (const float*)(b + off_a[4]); s.qz4 = (const float*)(b + off_a[5]);
+  s.qnx = (const float*)(b + off_a[6]); s.qny = (const float*)(b + off_a[7]); s.qnz = (const float*)(b + off_a[8]);
+  return PF_OK;
+}
+
+static size_t x_smem(int nx, int nF, int wy) {
+  int pitch;
+  switch (nx) {
+    case 16: pitch = Line<8>::PITCH; break;
+    case 32: pitch = Line<16>::PITCH; break;
+    case 64: pitch = Line<32>::PITCH; break;
+    case 128: pitch = Line<64>::PITCH; break;
+    case 256: pitch = Line<128>::PITCH; break;
+    default: return 0;
+  }
+  return (size_t)nF * wy * pitch * sizeof(float2);
+}
+
+static const size_t kMaxSmem = 227 * 1024;
+
+static int validate(const pf_config* c) {
+  if (!c) return fail(PF_EINVAL, "null config");
+  XKernels xk;
+  YZKernels yk;
+  if (!get_x_kernels(c->nx, &xk)) return fail(PF_EINVAL, "Nx=%d not supported (16, 32, 64, 128, 256)", c->nx);
+  if (!get_yz_kernels(c->ny, c->nz, &yk))
+    return fail(PF_EINVAL, "(Ny, Nz)=(%d, %d) not supported by the fused FP32 path", c->ny, c->nz);
+  if (c->ny % xk.wy != 0) return fail(PF_EINVAL, "Ny=%d must be a multiple of %d for Nx=%d", c->ny, xk.wy, c->nx);
+  if (c->var < 1 || c->var > 48) return fail(PF_EINVAL, "var=%d outside [1, 48]", c->var);
+  if (x_smem(c->nx, c->var + 1, xk.wy) > kMaxSmem)
+    return fail(PF_EINVAL, "var=%d too large for Nx=%d (shared memory)", c->var, c->nx);
+  if (c->mobility != PF_MOB_REFERENCE && c->mobility != PF_MOB_C1MC)
+    return fail(PF_EINVAL, "unknown mobility form %d", c->mobility);
+  if (!std::isfinite(c->t_step)) return fail(PF_EINVAL, "t_step not finite");
+  return PF_OK;
+}
+
+static int mob_mode(const pf_config* c) {
+  if (c->mobility == PF_MOB_C1MC) return MOB_C1MC;
+  return c->D_gb == 0.0 ? MOB_CONST : MOB_REF_VAR;
+}
+
+}  // namespace pf
+
+using namespace pf;
+
+// ---------------------------------------------------------------------------
+// Batch = one or more same-shape runs stepped by one set of launches
+// ---------------------------------------------------------------------------
+struct pf_batch {
+  int nruns = 0;
+  int device = 0;
+  int Nx = 0, Ny = 0, Nz = 0, V = 0, nF = 0, Kx = 0;
+  int mob = MOB_CONST;
+  DevTables tab;
+  XKernels xk{};
+  YZKernels yk{};
+  size_t smem_x = 0, smem_xj = 0;
+  std::vector<RunParams> hrp;
+  RunParams* drp = nullptr;
+  void* mem = nullptr;         // all per-run buffers
+  float* fin = nullptr;        // float staging [nF][Nz][Ny][Nx]
+  double* dstage = nullptr;    // double staging for one run's AoS fields
+  int ring = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<double> hdiag;
+  std::vector<int> steps_done;
+};
+
+struct pf_run {
+  int precision = PF_FP32_FUSED;
+  pf_batch* b = nullptr;
+  pf::Plain64* p64 = nullptr;
+};
+
+static int enqueue_step(pf_batch* b, cudaStream_t s) {
+  const Shape sh = b->tab.sh;
+  const int R = b->nruns;
+  const dim3 gx(b->Nz * (b->Ny / b->xk.wy), R);
+  b->xk.bulk<<<gx, 256, b->smem_x, s>>>(b->drp, sh);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = b->yk.cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(b->yk.cluster * b->nF * b->Kx, R);
+  cfg.blockDim = dim3(b->yk.threads);
+  cfg.dynamicSmemBytes = b->yk.smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  PF_CUDA(cudaLaunchKernelEx(&cfg, b->yk.main, (const RunParams*)b->drp, sh));
+  if (b->mob != MOB_CONST) {
+    b->xk.xj<<<gx, 256, b->smem_xj, s>>>(b->drp, sh);
+    cfg.gridDim = dim3(b->yk.cluster * b->Kx, R);
+    PF_CUDA(cudaLaunchKernelEx(&cfg, b->yk.c2, (const RunParams*)b->drp, sh));
+  }
+  reduce_diag_kernel<<<R, 256, 0, s>>>(b->drp, sh);
+  PF_CUDA(cudaGetLastError());
+  return PF_OK;
+}
+
+static void destroy_batch(pf_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  cudaFree(b->drp);
+  cudaFree(b->mem);
+  cudaFree(b->fin);
+  cudaFree(b->dstage);
+  cudaFree(b->tab.base);
+  delete b;
+}
+
+static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
+  if (!out) return fail(PF_EINVAL, "null output pointer");
+  *out = nullptr;
+  if (nruns < 1 || nruns > 65535) return fail(PF_EINVAL, "nruns=%d outside [1, 65535]", nruns);
+  for (int i = 0; i < nruns; ++i) {
+    int rc = validate(&cfgs[i]);
+    if (rc) return rc;
+    const pf_config& a = cfgs[0];
+    const pf_config& c = cfgs[i];
+    if (c.nx != a.nx || c.ny != a.ny || c.nz != a.nz || c.var != a.var || c.device != a.device)
+      return fail(PF_EINVAL, "run %d: all runs of a batch need the same grid, var and device", i);
+    if ((mob_mode(&c) == MOB_CONST) != (mob_mode(&a) == MOB_CONST))
+      return fail(PF_EINVAL, "run %d: constant- and variable-mobility runs cannot share a batch", i);
+  }
+  pf_batch* b = new pf_batch();
+  const pf_config& c0 = cfgs[0];
+  b->nruns = nruns;
+  b->device = c0.device;
+  b->Nx = c0.nx; b->Ny = c0.ny; b->Nz = c0.nz; b->V = c0.var; b->nF = c0.var + 1; b->Kx = c0.nx / 2 + 1;
+  b->mob = mob_mode(&c0);
+  for (int i = 0; i < nruns; ++i)
+    if (mob_mode(&cfgs[i]) != MOB_CONST) b->mob = mob_mode(&cfgs[i]);
+  get_x_kernels(b->Nx, &b->xk);
+  get_yz_kernels(b->Ny, b->Nz, &b->yk);
+  b->smem_x = x_smem(b->Nx, b->nF, b->xk.wy);
+  b->smem_xj = x_smem(b->Nx, 1, b->xk.wy);
+  auto bail = [&](int rc) { destroy_batch(b); return rc; };
+  cudaError_t e = cudaSetDevice(b->device);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "cudaSetDevice(%d): %s", b->device, cudaGetErrorString(e)));
+  int rc = build_tables(b->Nx, b->Ny, b->Nz, b->tab);
+  if (rc) return bail(rc);
+  Shape& sh = b->tab.sh;
+  sh.nblk_x = b->Nz * (b->Ny / b->xk.wy);
+  sh.nblk_yz = b->yk.cluster * b->nF * b->Kx;
+
+  // kernel attributes (idempotent)
+  KernelFn xs[4] = {b->xk.bulk, b->xk.xj, b->xk.imp, b->xk.exp};
+  for (KernelFn k : xs) {
+    e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem_x);
+    if (e != cudaSuccess) return bail(fail(PF_ECUDA, "x-pass smem attribute: %s", cudaGetErrorString(e)));
+  }
+  for (KernelFn k : {b->yk.main, b->yk.c2}) {
+    e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->yk.smem);
+    if (e != cudaSuccess) return bail(fail(PF_ECUDA, "yz-pass smem attribute: %s", cudaGetErrorString(e)));
+    if (b->yk.cluster > 8) {
+      e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      if (e != cudaSuccess) return bail(fail(PF_ECUDA, "cluster attribute: %s", cudaGetErrorString(e)));
+    }
+  }
+  {
+    // the cluster shape must be schedulable on this device
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = b->yk.cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(b->yk.cluster * b->nF * b->Kx, 1);
+    cfg.blockDim = dim3(b->yk.threads);
+    cfg.dynamicSmemBytes = b->yk.smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    e = cudaOccupancyMaxActiveClusters(&ncl, (const void*)b->yk.main, &cfg);
+    if (e != cudaSuccess || ncl < 1)
+      return bail(fail(PF_ECUDA, "yz cluster of %d CTAs with %zu B smem cannot be scheduled: %s", b->yk.cluster,
+                       b->yk.smem, cudaGetErrorString(e)));
+  }
+
+  // buffers
+  const size_t plane = (size_t)b->Ny * b->Nz;
+  const size_t fieldc = (size_t)b->Kx * plane;  // complex elements per field
+  const size_t ncell = (size_t)b->Nx * b->Ny * b->Nz;
+  const bool var = b->mob != MOB_CONST;
+  b->ring = 1024;
+  auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const size_t szS = align(b->nF * fieldc * sizeof(float2));
+  const size_t szMob = var ? align(ncell * sizeof(float)) : 0;
+  const size_t szJ = var ? align(fieldc * sizeof(float2)) : 0;
+  const size_t szPx = align((size_t)XD_COUNT * sh.nblk_x * sizeof(double));
+  const size_t szPyz = align((size_t)sh.nblk_yz * sizeof(double));
+  const size_t szDiag = align((size_t)b->ring * DR_COUNT * sizeof(double));
+  const size_t szCnt = 256;
+  const size_t per_run = 2 * szS + szMob + 2 * szJ + szPx + szPyz + szDiag + szCnt;
+  e = cudaMalloc(&b->mem, per_run * nruns);
+  if (e != cudaSuccess)
+    return bail(fail(PF_ENOMEM, "cudaMalloc(%zu bytes) for %d runs: %s", per_run * nruns, nruns, cudaGetErrorString(e)));
+  e = cudaMemset(b->mem, 0, per_run * nruns);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "cudaMemset: %s", cudaGetErrorString(e)));
+  e = cudaMalloc(&b->fin, b->nF * ncell * sizeof(float));
+  if (e != cudaSuccess) return bail(fail(PF_ENOMEM, "staging allocation: %s", cudaGetErrorString(e)));
+  e = cudaMalloc(&b->dstage, b->nF * ncell * sizeof(double));
+  if (e != cudaSuccess) return bail(fail(PF_ENOMEM, "staging allocation: %s", cudaGetErrorString(e)));
+  b->hrp.resize(nruns);
+  b->steps_done.assign(nruns, 0);
+  for (int i = 0; i < nruns; ++i) {
+    const pf_config& c = cfgs[i];
+    char* p = (char*)b->mem + per_run * i;
+    RunParams& r = b->hrp[i];
+    memset(&r, 0, sizeof r);
+    r.S = (float2*)p; p += szS;
+    r.D = (float2*)p; p += szS;
+    r.mob = var ? (float*)p : nullptr; p += szMob;
+    r.J = var ? (float2*)p : nullptr; p += szJ;
+    r.A = var ? (float2*)p : nullptr; p += szJ;
+    r.part_x = (double*)p; p += szPx;
+    r.part_yz = (double*)p; p += szPyz;
+    r.diag = (double*)p; p += szDiag;
+    r.counter = (int*)p;
+    r.fin = b->fin;
+    r.L = (float)c.mob_phi;
+    r.kappa_phi = (float)c.grad_coeff_phi;
+    r.kappa_c = (float)c.grad_coeff_c;
+    r.dt = (float)c.t_step;
+    r.D_L = (float)c.D_L;
+    r.D_gb = (float)c.D_gb;
+    r.sigma1 = (float)c.sigma_1;
+    r.sigma2 = (float)c.sigma_2;
+    r.am = (float)c.am;
+    r.ap = (float)c.ap;
+    r.c0m = (float)c.con_0_mat;
+    r.c0p = (float)c.con_0_ppt;
+    r.mobility = mob_mode(&c);
+    r.V = c.var;
+    r.ring = b->ring;
+  }
+  e = cudaMalloc(&b->drp, nruns * sizeof(RunParams));
+  if (e != cudaSuccess) return bail(fail(PF_ENOMEM, "run table: %s", cudaGetErrorString(e)));
+  e = cudaMemcpy(b->drp, b->hrp.data(), nruns * sizeof(RunParams), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "run table copy: %s", cudaGetErrorString(e)));
+  e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream: %s", cudaGetErrorString(e)));
+
+  // capture one step as a CUDA graph
+  cudaGraph_t g = nullptr;
+  e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "begin capture: %s", cudaGetErrorString(e)));
+  rc = enqueue_step(b, b->stream);
+  cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+  if (rc) { if (g) cudaGraphDestroy(g); return bail(rc); }
+  if (e2 != cudaSuccess) return bail(fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2)));
+  e = cudaGraphInstantiate(&b->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)));
+  *out = b;
+  return PF_OK;
+}
+
+static int batch_set_fields(pf_batch* b, int run, const double* phi, const double* con) {
+  if (!b || run < 0 || run >= b->nruns || !phi || !con) return fail(PF_EINVAL, "bad arguments to set_fields");
+  PF_CUDA(cudaSetDevice(b->device));
+  const size_t ncell = (size_t)b->Nx * b->Ny * b->Nz;
+  double* dphi = b->dstage;
+  double* dcon = b->dstage + (size_t)b->V * ncell;
+  PF_CUDA(cudaMemcpyAsync(dphi, phi, (size_t)b->V * ncell * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  PF_CUDA(cudaMemcpyAsync(dcon, con, ncell * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  aos_to_soa_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, b->stream>>>(dphi, dcon, b->fin, b->V, ncell);
+  const dim3 gx(b->Nz * (b->Ny / b->xk.wy), 1);
+  b->xk.imp<<<gx, 256, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
+  PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, sizeof(int), b->stream));
+  PF_CUDA(cudaGetLastError());
+  PF_CUDA(cudaStreamSynchronize(b->stream));
+  b->steps_done[run] = 0;
+  return PF_OK;
+}
+
+static int batch_get_fields(pf_batch* b, int run, double* phi, double* con) {
+  if (!b || run < 0 || run >= b->nruns || !phi || !con) return fail(PF_EINVAL, "bad arguments to get_fields");
+  PF_CUDA(cudaSetDevice(b->device));
+  const size_t ncell = (size_t)b->Nx * b->Ny * b->Nz;
+  double* dphi = b->dstage;
+  double* dcon = b->dstage + (size_t)b->V * ncell;
+  const dim3 gx(b->Nz * (b->Ny / b->xk.wy), 1);
+  b->xk.exp<<<gx, 256, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
+  soa_to_aos_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, b->stream>>>(b->fin, dphi, dcon, b->V, ncell);
+  PF_CUDA(cudaGetLastError());
+  PF_CUDA(cudaMemcpyAsync(phi, dphi, (size_t)b->V * ncell * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  PF_CUDA(cudaMemcpyAsync(con, dcon, ncell * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  PF_CUDA(cudaStreamSynchronize(b->stream));
+  return PF_OK;
+}
+
+static void fill_diag(const double* d, pf_diag* o) {
+  o->step = (int)d[DR_STEP];
+  o->nonfinite = (int)d[DR_NONFINITE];
+  o->f_int = d[DR_FINT];
+  o->f_eta = d[DR_FETA];
+  o->f_ch = d[DR_FCH];
+  o->e_tot = d[DR_FINT] + d[DR_FCH] + d[DR_FETA];  // src/var_diff.f90:1070
+  o->c_max = d[DR_CMAX];
+  o->c_min = d[DR_CMIN];
+  o->phi_min = d[DR_PHIMIN];
+  o->phi_P_max = d[DR_PHIPMAX];
+  o->mass = d[DR_MASS];
+}
+
+static int batch_step(pf_batch* b, int nsteps, pf_diag* diag) {
+  if (!b || nsteps < 0) return fail(PF_EINVAL, "bad arguments to step");
+  PF_CUDA(cudaSetDevice(b->device));
+  int bad = 0;
+  int done = 0;
+  while (done < nsteps) {
+    const int chunk = std::min(nsteps - done, b->ring);
+    for (int s = 0; s < chunk; ++s) PF_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    PF_CUDA(cudaStreamSynchronize(b->stream));
+    b->hdiag.resize((size_t)b->ring * DR_COUNT);
+    for (int r = 0; r < b->nruns; ++r) {
+      PF_CUDA(cudaMemcpy(b->hdiag.data(), b->hrp[r].diag, (size_t)b->ring * DR_COUNT * sizeof(double),
+                         cudaMemcpyDeviceToHost));
+      for (int s = 0; s < chunk; ++s) {
+        const int step = b->steps_done[r] + s;  // 0-based
+        const double* d = b->hdiag.data() + (size_t)(step % b->ring) * DR_COUNT;
+        if (d[DR_NONFINITE] != 0) bad = 1;
+        if (diag) fill_diag(d, &diag[(size_t)r * nsteps + done + s]);
+      }
+      b->steps_done[r] += chunk;
+    }
+    done += chunk;
+  }
+  if (bad) return fail(PF_ENONFINITE, "a step produced non-finite values");
+  return PF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// exported C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* pf_last_error(void) { return g_err.c_str(); }
+
+int pf_supported_shape(int nx, int ny, int nz, int var, int precision) {
+  pf_config c;
+  memset(&c, 0, sizeof c);
+  c.nx = nx; c.ny = ny; c.nz = nz; c.var = var; c.precision = precision; c.t_step = 0.1;
+  std::string keep = g_err;
+  int ok;
+  if (precision == PF_FP64_PLAIN) ok = plain64_validate(&c) == PF_OK;
+  else ok = validate(&c) == PF_OK;
+  g_err = keep;
+  return ok;
+}
+
+int pf_create(const pf_config* cfg, pf_run** out) {
+  if (!cfg || !out) return fail(PF_EINVAL, "null argument");
+  *out = nullptr;
+  pf_run* r = new pf_run();
+  r->precision = cfg->precision;
+  int rc;
+  if (cfg->precision == PF_FP64_PLAIN) rc = plain64_create(cfg, &r->p64);
+  else if (cfg->precision == PF_FP32_FUSED || cfg->precision == 0) {
+    r->precision = PF_FP32_FUSED;
+    rc = create_batch(cfg, 1, &r->b);
+  } else rc = fail(PF_EINVAL, "unknown precision %d", cfg->precision);
+  if (rc) { delete r; return rc; }
+  *out = r;
+  return PF_OK;
+}
+
+int pf_set_fields(pf_run* run, const double* phi, const double* con) {
+  if (!run) return fail(PF_EINVAL, "null run");
+  if (run->p64) return plain64_set_fields(run->p64, phi, con);
+  return batch_set_fields(run->b, 0, phi, con);
+}
+
+int pf_step(pf_run* run, int nsteps, pf_diag* diag) {
+  if (!run) return fail(PF_EINVAL, "null run");
+  if (run->p64) return plain64_step(run->p64, nsteps, diag);
+  return batch_step(run->b, nsteps, diag);
+}
+
+int pf_get_fields(pf_run* run, double* phi, double* con) {
+  if (!run) return fail(PF_EINVAL, "null run");
+  if (run->p64) return plain64_get_fields(run->p64, phi, con);
+  return batch_get_fields(run->b, 0, phi, con);
+}
+
+int pf_destroy(pf_run* run) {
+  if (!run) return PF_OK;
+  if (run->p64) plain64_destroy(run->p64);
+  destroy_batch(run->b);
+  delete run;
+  return PF_OK;
+}
+
+int pf_batch_create(const pf_config* cfgs, int nruns, pf_batch** out) {
+  if (!cfgs) return fail(PF_EINVAL, "null configs");
+  for (int i = 0; i < nruns; ++i)
+    if (cfgs[i].precision != PF_FP32_FUSED && cfgs[i].precision != 0)
+      return fail(PF_EINVAL, "batches run on the fused FP32 path only");
+  return create_batch(cfgs, nruns, out);
+}
+int pf_batch_set_fields(pf_batch* b, int run, const double* phi, const double* con) {
+  return batch_set_fields(b, run, phi, con);
+}
+int pf_batch_step(pf_batch* b, int nsteps, pf_diag* diag) { return batch_step(b, nsteps, diag); }
+int pf_batch_get_fields(pf_batch* b, int run, double* phi, double* con) { return batch_get_fields(b, run, phi, con); }
+int pf_batch_destroy(pf_batch* b) {
+  destroy_batch(b);
+  return PF_OK;
+}
+
+// Internal hooks for the benchmark: enqueue steps / query the stream without
+// host synchronisation.  Not part of the public header.
+int pf_batch_enqueue(pf_batch* b, int nsteps) {
+  if (!b) return fail(PF_EINVAL, "null batch");
+  PF_CUDA(cudaSetDevice(b->device));
+  for (int s = 0; s < nsteps; ++s) PF_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+  for (int r = 0; r < b->nruns; ++r) b->steps_done[r] += nsteps;
+  return PF_OK;
+}
+void* pf_batch_stream(pf_batch* b) { return b ? (void*)b->stream : nullptr; }
+pf_batch* pf_run_batch(pf_run* r) { return r ? r->b : nullptr; }
+// Launch the x pass / yz pass alone (kernel timing); returns PF_OK.
+int pf_batch_enqueue_phase(pf_batch* b, int phase) {
+  if (!b) return fail(PF_EINVAL, "null batch");
+  const Shape sh = b->tab.sh;
+  const dim3 gx(b->Nz * (b->Ny / b->xk.wy), b->nruns);
+  if (phase == 0) {
+    b->xk.bulk<<<gx, 256, b->smem_x, b->stream>>>(b->drp, sh);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = b->yk.cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(b->yk.cluster * b->nF * b->Kx, b->nruns);
+    cfg.blockDim = dim3(b->yk.threads);
+    cfg.dynamicSmemBytes = b->yk.smem;
+    cfg.stream = b->stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    PF_CUDA(cudaLaunchKernelEx(&cfg, b->yk.main, (const RunParams*)b->drp, sh));
+  }
+  PF_CUDA(cudaGetLastError());
+  return PF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,278 @@
+// Shared-memory FFT building blocks for the sm_103a phase-field step.
+//
+// These replace the FFTs that the reference obtains from P3DFFT/FFTW through
+// f_trans (src/f_trans.f90:11, forward R2C) and inv_trans
+// (src/inv_trans.f90:10, inverse C2R).  A line of length L = N1*N2 is
+// transformed in place by a two-pass "four-step" algorithm:
+//
+//   pass A (per column n1 < N1):  V = DFT_N2(x[n1 + N1*n2]),  x[n1+N1*k2] = V[k2]*W_L^(n1*k2)
+//   pass B (per row    k2 < N2):  x[k1+N1*k2] = DFT_N1(x[n1+N1*k2])[k1]
+//
+// so that after the forward transform position p = k1 + N1*k2 holds the
+// coefficient of frequency k = k2 + N2*k1 ("digit-transposed" order).  The
+// inverse runs the same passes backwards (B then A, conjugate twiddles) and
+// takes that order back to natural order.  The spectral update in between is
+// pointwise, so no reordering pass is ever needed.
+//
+// Each DFT of size <= 16 lives in registers; in shared memory every run of N1
+// consecutive elements is followed by one pad slot and the line pitch is odd,
+// which makes pass A, pass B and line-to-line transposes free of bank
+// conflicts for 8-byte complex elements.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace pf {
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+// a * b
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+// -i * a
+__device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
+// +i * a
+__device__ __forceinline__ float2 cmul_pi(float2 a) { return make_float2(-a.y, a.x); }
+
+// ---------------------------------------------------------------------------
+// Exact twiddle constants for the in-register DFTs (W_R^j = e^{-2 pi i j / R})
+// ---------------------------------------------------------------------------
+#define PF_C16_1 0.92387953251128675613f  // cos(pi/8)
+#define PF_S16_1 0.38268343236508977173f  // sin(pi/8)
+#define PF_SQRT1_2 0.70710678118654752440f
+#define PF_SQRT3_2 0.86602540378443864676f
+
+// W_R^j for R in {2,3,4,6,8,12,16} (forward sign), j in [0, R)
+template <int R>
+__device__ __forceinline__ float2 wconst(int j);
+
+template <>
+__device__ __forceinline__ float2 wconst<16>(int j) {
+  // angles j * 22.5 degrees, clockwise
+  const float c[16] = {1.f, PF_C16_1, PF_SQRT1_2, PF_S16_1, 0.f, -PF_S16_1, -PF_SQRT1_2, -PF_C16_1,
+                       -1.f, -PF_C16_1, -PF_SQRT1_2, -PF_S16_1, 0.f, PF_S16_1, PF_SQRT1_2, PF_C16_1};
+  return make_float2(c[j & 15], -c[(j + 12) & 15]);
+}
+template <>
+__device__ __forceinline__ float2 wconst<8>(int j) { return wconst<16>(2 * j); }
+template <>
+__device__ __forceinline__ float2 wconst<4>(int j) { return wconst<16>(4 * j); }
+template <>
+__device__ __forceinline__ float2 wconst<12>(int j) {
+  // angles j * 30 degrees, clockwise
+  const float c[12] = {1.f, PF_SQRT3_2, 0.5f, 0.f, -0.5f, -PF_SQRT3_2, -1.f, -PF_SQRT3_2, -0.5f, 0.f, 0.5f, PF_SQRT3_2};
+  return make_float2(c[j % 12], -c[(j + 9) % 12]);
+}
+template <>
+__device__ __forceinline__ float2 wconst<6>(int j) { return wconst<12>(2 * j); }
+template <>
+__device__ __forceinline__ float2 wconst<3>(int j) { return wconst<12>(4 * j); }
+
+// ---------------------------------------------------------------------------
+// In-register forward DFTs, natural order in and out
+// ---------------------------------------------------------------------------
+template <int R>
+struct Dft;
+
+template <>
+struct Dft<1> {
+  __device__ __forceinline__ static void fwd(float2*) {}
+};
+
+template <>
+struct Dft<2> {
+  __device__ __forceinline__ static void fwd(float2* v) {
+    float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <>
+struct Dft<3> {
+  __device__ __forceinline__ static void fwd(float2* v) {
+    float2 a = v[0];
+    float2 t1 = cadd(v[1], v[2]);
+    float2 t2 = csub(v[1], v[2]);
+    float2 m = make_float2(fmaf(-0.5f, t1.x, a.x), fmaf(-0.5f, t1.y, a.y));
+    float2 s = cscale(t2, PF_SQRT3_2);
+    v[0] = cadd(a, t1);
+    v[1] = cadd(m, cmul_mi(s));
+    v[2] = cadd(m, cmul_pi(s));
+  }
+};
+
+template <>
+struct Dft<4> {
+  __device__ __forceinline__ static void fwd(float2* v) {
+    float2 t0 = cadd(v[0], v[2]);
+    float2 t1 = csub(v[0], v[2]);
+    float2 t2 = cadd(v[1], v[3]);
+    float2 t3 = cmul_mi(csub(v[1], v[3]));
+    v[0] = cadd(t0, t2);
+    v[2] = csub(t0, t2);
+    v[1] = cadd(t1, t3);
+    v[3] = csub(t1, t3);
+  }
+};
+
+// Composite R = R1*R2 in registers: x[n1 + R1*n2] -> X[k2 + R2*k1]
+template <int R1, int R2>
+struct DftComposite {
+  static constexpr int R = R1 * R2;
+  __device__ __forceinline__ static void fwd(float2* v) {
+    float2 t[R];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) {
+      float2 c[R2];
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) c[n2] = v[n1 + R1 * n2];
+      Dft<R2>::fwd(c);
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) {
+        float2 w = wconst<R>(n1 * k2);
+        t[n1 + R1 * k2] = (n1 * k2 == 0) ? c[k2] : cmul(c[k2], w);
+      }
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) {
+      float2 r[R1];
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) r[n1] = t[n1 + R1 * k2];
+      Dft<R1>::fwd(r);
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) v[k2 + R2 * k1] = r[k1];
+    }
+  }
+};
+
+template <>
+struct Dft<6> {
+  __device__ __forceinline__ static void fwd(float2* v) { DftComposite<2, 3>::fwd(v); }
+};
+template <>
+struct Dft<8> {
+  __device__ __forceinline__ static void fwd(float2* v) { DftComposite<2, 4>::fwd(v); }
+};
+template <>
+struct Dft<12> {
+  __device__ __forceinline__ static void fwd(float2* v) { DftComposite<4, 3>::fwd(v); }
+};
+template <>
+struct Dft<16> {
+  __device__ __forceinline__ static void fwd(float2* v) { DftComposite<4, 4>::fwd(v); }
+};
+
+// Inverse (unnormalised, e^{+2 pi i jk/R}) via conj(DFT(conj(x)))
+template <int R>
+__device__ __forceinline__ void dft_inv(float2* v) {
+#pragma unroll
+  for (int i = 0; i < R; ++i) v[i].y = -v[i].y;
+  Dft<R>::fwd(v);
+#pragma unroll
+  for (int i = 0; i < R; ++i) v[i].y = -v[i].y;
+}
+
+// ---------------------------------------------------------------------------
+// Line plans
+// ---------------------------------------------------------------------------
+template <int L>
+struct Plan;
+// (N1 = contiguous run length of pass B, N2 = stride count of pass A)
+template <> struct Plan<4>   { static constexpr int N1 = 2,  N2 = 2; };
+template <> struct Plan<8>   { static constexpr int N1 = 4,  N2 = 2; };
+template <> struct Plan<12>  { static constexpr int N1 = 4,  N2 = 3; };
+template <> struct Plan<16>  { static constexpr int N1 = 4,  N2 = 4; };
+template <> struct Plan<24>  { static constexpr int N1 = 8,  N2 = 3; };
+template <> struct Plan<32>  { static constexpr int N1 = 8,  N2 = 4; };
+template <> struct Plan<48>  { static constexpr int N1 = 8,  N2 = 6; };
+template <> struct Plan<64>  { static constexpr int N1 = 8,  N2 = 8; };
+template <> struct Plan<96>  { static constexpr int N1 = 8,  N2 = 12; };
+template <> struct Plan<128> { static constexpr int N1 = 16, N2 = 8; };
+template <> struct Plan<192> { static constexpr int N1 = 16, N2 = 12; };
+template <> struct Plan<256> { static constexpr int N1 = 16, N2 = 16; };
+
+template <int L>
+struct Line {
+  static constexpr int N1 = Plan<L>::N1;
+  static constexpr int N2 = Plan<L>::N2;
+  static_assert(N1 * N2 == L, "bad plan");
+  // padded storage: one pad slot after every run of N1, odd line pitch
+  static constexpr int RAW = N2 * (N1 + 1);
+  static constexpr int PITCH = (RAW % 2 == 1) ? RAW : RAW + 1;
+  __device__ __forceinline__ static int phys(int j) { return j + j / N1; }
+  // frequency held at (natural) position p after a forward transform
+  __device__ __forceinline__ static int freq_of_pos(int p) { return p / N1 + N2 * (p % N1); }
+  __device__ __forceinline__ static int pos_of_freq(int k) { return k / N2 + N1 * (k % N2); }
+};
+
+// Forward transform of `nlines` lines of length L stored at buf + l*pitch
+// (phys() layout inside each line).  tw = W_L^j, j in [0, L), from a table.
+// Must be called by all threads of the block; ends with __syncthreads().
+template <int L>
+__device__ __forceinline__ void fft_fwd_lines(float2* buf, int nlines, int pitch, const float2* __restrict__ tw) {
+  using Ln = Line<L>;
+  constexpr int N1 = Ln::N1, N2 = Ln::N2;
+  for (int it = threadIdx.x; it < nlines * N1; it += blockDim.x) {
+    const int l = it / N1, n1 = it - l * N1;
+    float2* p = buf + l * pitch + n1;
+    float2 v[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) v[n2] = p[n2 * (N1 + 1)];
+    Dft<N2>::fwd(v);
+#pragma unroll
+    for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], __ldg(tw + n1 * k2));
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) p[k2 * (N1 + 1)] = v[k2];
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < nlines * N2; it += blockDim.x) {
+    const int l = it / N2, k2 = it - l * N2;
+    float2* p = buf + l * pitch + k2 * (N1 + 1);
+    float2 u[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) u[n1] = p[n1];
+    Dft<N1>::fwd(u);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) p[k1] = u[k1];
+  }
+  __syncthreads();
+}
+
+// Inverse (unnormalised) transform: digit-transposed in, natural out.
+template <int L>
+__device__ __forceinline__ void fft_inv_lines(float2* buf, int nlines, int pitch, const float2* __restrict__ tw) {
+  using Ln = Line<L>;
+  constexpr int N1 = Ln::N1, N2 = Ln::N2;
+  for (int it = threadIdx.x; it < nlines * N2; it += blockDim.x) {
+    const int l = it / N2, k2 = it - l * N2;
+    float2* p = buf + l * pitch + k2 * (N1 + 1);
+    float2 u[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) u[n1] = p[n1];
+    dft_inv<N1>(u);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) p[k1] = u[k1];
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < nlines * N1; it += blockDim.x) {
+    const int l = it / N1, n1 = it - l * N1;
+    float2* p = buf + l * pitch + n1;
+    float2 v[N2];
+    v[0] = p[0];
+#pragma unroll
+    for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * (N1 + 1)], __ldg(tw + n1 * k2));
+    dft_inv<N2>(v);
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) p[n2 * (N1 + 1)] = v[n2];
+  }
+  __syncthreads();
+}
+
+}  // namespace pf

@@ -1,0 +1,246 @@
+"""ctypes binding of libpfgpu.so (include/pfgpu.h).
+
+Field arrays on the Python side use the layout ``phi[ivar, z, y, x]`` and
+``con[z, y, x]`` (C order, x fastest); they are converted to the Fortran
+``phi(var, x, y, z)`` order of the C ABI on the way in and out.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+PF_OK, PF_EINVAL, PF_ECUDA, PF_ENOMEM, PF_ENONFINITE, PF_EIO = 0, -1, -2, -3, -4, -5
+PF_MOB_REFERENCE, PF_MOB_C1MC = 0, 1
+PF_FP32_FUSED, PF_FP64_PLAIN = 32, 64
+
+EXPORTED = (
+    "pf_create", "pf_supported_shape", "pf_set_fields", "pf_step", "pf_get_fields", "pf_destroy",
+    "pf_last_error", "pf_batch_create", "pf_batch_set_fields", "pf_batch_step", "pf_batch_get_fields",
+    "pf_batch_destroy", "f_trans_", "inv_trans_", "k_space_", "pf_shim_device", "pf_ran2_init", "pf_ran2",
+)
+
+
+class PFError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"pfgpu error {code}: {msg}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("var", C.c_int),
+        ("t_step", C.c_double), ("grad_coeff_phi", C.c_double), ("grad_coeff_c", C.c_double),
+        ("D_S", C.c_double), ("D_L", C.c_double), ("D_gb", C.c_double), ("mob_phi", C.c_double),
+        ("sigma_1", C.c_double), ("sigma_2", C.c_double),
+        ("am", C.c_double), ("ap", C.c_double), ("con_0_mat", C.c_double), ("con_0_ppt", C.c_double),
+        ("mobility", C.c_int), ("precision", C.c_int), ("device", C.c_int), ("reserved", C.c_int * 5),
+    ]
+
+
+class Diag(C.Structure):
+    _fields_ = [
+        ("step", C.c_int), ("nonfinite", C.c_int),
+        ("f_int", C.c_double), ("f_eta", C.c_double), ("f_ch", C.c_double), ("e_tot", C.c_double),
+        ("c_max", C.c_double), ("c_min", C.c_double), ("phi_min", C.c_double), ("phi_P_max", C.c_double),
+        ("mass", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Ran2State(C.Structure):
+    _fields_ = [("idum2", C.c_int), ("iy", C.c_int), ("iv", C.c_int * 32), ("initialised", C.c_int),
+                ("pad", C.c_int * 5)]
+
+
+_LIB = None
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load_library(build_if_missing: bool = True) -> C.CDLL:
+    """Load (building first if needed) the in-tree libpfgpu.so."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not path.exists():
+        if not build_if_missing:
+            raise FileNotFoundError(f"{path} is missing: run build() first")
+        _build.build()
+    lib = C.CDLL(str(path))
+    P = C.POINTER
+    dp = P(C.c_double)
+    ip = P(C.c_int)
+    sig = {
+        "pf_create": (C.c_int, [P(Config), P(C.c_void_p)]),
+        "pf_supported_shape": (C.c_int, [C.c_int] * 5),
+        "pf_set_fields": (C.c_int, [C.c_void_p, dp, dp]),
+        "pf_step": (C.c_int, [C.c_void_p, C.c_int, P(Diag)]),
+        "pf_get_fields": (C.c_int, [C.c_void_p, dp, dp]),
+        "pf_destroy": (C.c_int, [C.c_void_p]),
+        "pf_last_error": (C.c_char_p, []),
+        "pf_batch_create": (C.c_int, [P(Config), C.c_int, P(C.c_void_p)]),
+        "pf_batch_set_fields": (C.c_int, [C.c_void_p, C.c_int, dp, dp]),
+        "pf_batch_step": (C.c_int, [C.c_void_p, C.c_int, P(Diag)]),
+        "pf_batch_get_fields": (C.c_int, [C.c_void_p, C.c_int, dp, dp]),
+        "pf_batch_destroy": (C.c_int, [C.c_void_p]),
+        "pf_batch_enqueue": (C.c_int, [C.c_void_p, C.c_int]),
+        "pf_batch_enqueue_phase": (C.c_int, [C.c_void_p, C.c_int]),
+        "pf_batch_stream": (C.c_void_p, [C.c_void_p]),
+        "pf_run_batch": (C.c_void_p, [C.c_void_p]),
+        "f_trans_": (None, [dp, dp, ip, ip, ip, ip, ip, ip, ip]),
+        "inv_trans_": (None, [dp, dp, ip, ip, ip, ip]),
+        "k_space_": (None, [ip, ip, ip, ip, ip, dp, dp, dp]),
+        "pf_shim_device": (C.c_int, [C.c_int]),
+        "pf_ran2_init": (None, [P(Ran2State)]),
+        "pf_ran2": (C.c_double, [P(Ran2State), ip]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != PF_OK:
+        msg = load_library().pf_last_error().decode()
+        raise PFError(rc, msg)
+
+
+def make_config(p, precision: int = PF_FP32_FUSED, device: int = 0) -> Config:
+    """Config from any object with the input.txt attribute names (e.g. the
+    oracle's Params or the input-file reader's record)."""
+    c = Config()
+    c.nx, c.ny, c.nz, c.var = p.Nx, p.Ny, p.Nz, p.var
+    for k in ("t_step", "grad_coeff_phi", "grad_coeff_c", "D_S", "D_L", "D_gb", "mob_phi",
+              "sigma_1", "sigma_2", "am", "ap", "con_0_mat", "con_0_ppt"):
+        setattr(c, k, float(getattr(p, k)))
+    mob = getattr(p, "mobility", "reference")
+    c.mobility = PF_MOB_C1MC if mob in ("c1mc", PF_MOB_C1MC) else PF_MOB_REFERENCE
+    c.precision = precision
+    c.device = device
+    return c
+
+
+def to_aos(phi: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(np.moveaxis(np.asarray(phi, dtype=np.float64), 0, -1))
+
+
+def from_aos(buf: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(np.moveaxis(buf, -1, 0))
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Run:
+    """One run behind pf_create/pf_set_fields/pf_step/pf_get_fields."""
+
+    def __init__(self, params, precision: int = PF_FP32_FUSED, device: int = 0):
+        self.lib = load_library()
+        self.p = params
+        self.cfg = make_config(params, precision, device)
+        h = C.c_void_p()
+        _check(self.lib.pf_create(C.byref(self.cfg), C.byref(h)))
+        self.h = h
+
+    def set_fields(self, phi: np.ndarray, con: np.ndarray):
+        a = to_aos(phi)
+        c = np.ascontiguousarray(con, dtype=np.float64)
+        _check(self.lib.pf_set_fields(self.h, _dp(a), _dp(c)))
+
+    def step(self, n: int, raise_nonfinite: bool = True) -> List[dict]:
+        d = (Diag * max(n, 1))()
+        rc = self.lib.pf_step(self.h, n, d)
+        if rc != PF_ENONFINITE or raise_nonfinite:
+            _check(rc)
+        return [d[i].as_dict() for i in range(n)]
+
+    def get_fields(self):
+        p = self.p
+        a = np.empty((p.Nz, p.Ny, p.Nx, p.var))
+        c = np.empty((p.Nz, p.Ny, p.Nx))
+        _check(self.lib.pf_get_fields(self.h, _dp(a), _dp(c)))
+        return from_aos(a), c
+
+    def batch_handle(self):
+        return self.lib.pf_run_batch(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Same-shape runs stepped by one set of launches (pf_batch_*)."""
+
+    def __init__(self, params_list: Sequence, device: int = 0):
+        self.lib = load_library()
+        self.ps = list(params_list)
+        arr = (Config * len(self.ps))(*[make_config(p, PF_FP32_FUSED, device) for p in self.ps])
+        self._cfgs = arr
+        h = C.c_void_p()
+        _check(self.lib.pf_batch_create(arr, len(self.ps), C.byref(h)))
+        self.h = h
+
+    def set_fields(self, run: int, phi, con):
+        a = to_aos(phi)
+        c = np.ascontiguousarray(con, dtype=np.float64)
+        _check(self.lib.pf_batch_set_fields(self.h, run, _dp(a), _dp(c)))
+
+    def step(self, n: int) -> List[List[dict]]:
+        R = len(self.ps)
+        d = (Diag * max(R * n, 1))()
+        _check(self.lib.pf_batch_step(self.h, n, d))
+        return [[d[r * n + i].as_dict() for i in range(n)] for r in range(R)]
+
+    def get_fields(self, run: int):
+        p = self.ps[run]
+        a = np.empty((p.Nz, p.Ny, p.Nx, p.var))
+        c = np.empty((p.Nz, p.Ny, p.Nx))
+        _check(self.lib.pf_batch_get_fields(self.h, run, _dp(a), _dp(c)))
+        return from_aos(a), c
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pf_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ran2:
+    """The library's C restatement of ran_2 (for cross-checks and host ICs)."""
+
+    def __init__(self, idum: int):
+        self.lib = load_library()
+        self.st = Ran2State()
+        self.lib.pf_ran2_init(C.byref(self.st))
+        self.idum = C.c_int(idum)
+
+    def next(self) -> float:
+        return self.lib.pf_ran2(C.byref(self.st), C.byref(self.idum))
