@@ -59,16 +59,19 @@ def _run_lib(pkg, p, phi, con, steps, precision=32):
     return gp, gc, d
 
 
+# Parameter sets are kept inside the stable range of the explicit chemical and
+# variable-mobility terms (larger dt blows up in FP64 too); noise starts are
+# used only with am = ap = 0, where term4 is identically zero.
 CASES = {
     # name: (params kwargs, ic, steps)
     "c0_noise_32": (dict(Nx=32, Ny=32, Nz=32, var=4, t_step=0.05), ("noise", 0, 0.001, 0.5, 0.01), 100),
-    "chem_refvar_32": (dict(Nx=32, Ny=32, Nz=32, var=3, t_step=0.01, D_gb=1.0, am=0.5, ap=2.0, con_0_mat=0.3,
+    "chem_refvar_32": (dict(Nx=32, Ny=32, Nz=32, var=3, t_step=0.002, D_gb=1.0, am=0.5, ap=2.0, con_0_mat=0.3,
                             con_0_ppt=0.7, sigma_1=6.0, sigma_2=3.0), ("voronoi", 3, 5, 0.05, 0.5, 0.02), 50),
     "c1mc_32": (dict(Nx=32, Ny=32, Nz=32, var=4, t_step=0.1, mobility="c1mc"), ("voronoi", 1, 6, 0.01, 0.5, 0.02),
                 50),
-    "noncubic_64x32x64": (dict(Nx=64, Ny=32, Nz=64, var=2, t_step=0.05, am=0.5, ap=2.0, con_0_mat=0.3,
-                               con_0_ppt=0.7), ("noise", 5, 0.05, 0.5, 0.01), 30),
-    "noncubic_16x32x16": (dict(Nx=16, Ny=32, Nz=16, var=3, t_step=0.05, D_gb=0.5), ("noise", 6, 0.05, 0.5, 0.01),
+    "noncubic_64x32x64": (dict(Nx=64, Ny=32, Nz=64, var=2, t_step=0.005, am=0.5, ap=2.0, con_0_mat=0.3,
+                               con_0_ppt=0.7), ("voronoi", 5, 4, 0.05, 0.5, 0.01), 30),
+    "noncubic_16x32x16": (dict(Nx=16, Ny=32, Nz=16, var=3, t_step=0.005, D_gb=0.5), ("noise", 6, 0.05, 0.5, 0.01),
                           30),
     "cube16": (dict(Nx=16, Ny=16, Nz=16, var=5, t_step=0.05, mobility="c1mc"), ("voronoi", 7, 4, 0.01, 0.4, 0.02),
                40),
@@ -108,7 +111,7 @@ def test_fp32_config0_64cube_100_steps(pkg, oracle):
 
 
 def test_fp32_128cube_cluster(pkg, oracle):
-    p = oracle.Params(128, 128, 128, 2, t_step=0.1, mobility="c1mc", am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7)
+    p = oracle.Params(128, 128, 128, 2, t_step=0.02, mobility="c1mc", am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7)
     phi, con = oracle.ic_voronoi(p, 1, 8, 0.01, 0.5, 0.02)
     gp, gc, gd = _run_lib(pkg, p, phi, con, 6)
     op, oc, od = oracle.run(p, phi, con, 6, faithful=False, workers=8)
@@ -117,8 +120,8 @@ def test_fp32_128cube_cluster(pkg, oracle):
 
 
 def test_fp32_256cube_cluster(pkg, oracle):
-    p = oracle.Params(256, 256, 256, 1, t_step=0.1, am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7)
-    phi, con = oracle.ic_noise(p, 2, 0.05, 0.4, 0.02)
+    p = oracle.Params(256, 256, 256, 2, t_step=0.02, am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7)
+    phi, con = oracle.ic_voronoi(p, 2, 6, 0.01, 0.4, 0.02)
     gp, gc, gd = _run_lib(pkg, p, phi, con, 2)
     op, oc, od = oracle.run(p, phi, con, 2, faithful=False, workers=8)
     _check_fields(gp, gc, op, oc, TOL32)
