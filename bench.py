@@ -1,0 +1,349 @@
+#!/usr/bin/env python3
+"""Throughput of the fused FP32 phase-field step on one GB300 (or N replicas).
+
+Workload: the polycrystal run -- 128^3 periodic grid, 16 order parameters plus
+the concentration, 64 Voronoi grains from seed 1 with U(-0.01, 0.01) noise on
+every order parameter, c = 0.5 + U(-0.02, 0.02), concentration-dependent
+mobility M(c) = M0 (1 + c (1 - c)), a = b = 1, g = 1.5, kappa = 1, L = M0 = 1,
+dt = 0.1 (2000 steps for the full run).  One "step" is one semi-implicit time
+step of that run; the metric is cell-steps/s x P = Nx Ny Nz * P * steps / s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank steps its own independent replica (seed
+1 + rank) on its own GPU; there is no data-path collective ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+from types import SimpleNamespace
+
+ROOT = Path(__file__).resolve().parent
+WORKLOAD = dict(Nx=128, Ny=128, Nz=128, var=16, t_step=0.1, grad_coeff_phi=1.0, grad_coeff_c=1.0, D_S=1.0, D_L=1.0,
+                D_gb=0.0, mob_phi=1.0, sigma_1=1.5, sigma_2=1.5, am=0.0, ap=0.0, con_0_mat=0.0, con_0_ppt=1.0,
+                mobility="c1mc")
+IC = dict(seed=1, n_grains=64, amp_phi=0.01, c0=0.5, amp_c=0.02)
+WORKLOAD_NAME = "polycrystal 128^3, P=16, M(c)=M0(1+c(1-c)), 64 Voronoi grains seed 1, dt=0.1"
+METRIC = "cell-steps/s x P"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def params(**over):
+    d = dict(WORKLOAD)
+    d.update(over)
+    return SimpleNamespace(**d)
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel_key: str):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "ncu_traffic.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel_key:
+            try:
+                return int(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_port_throughput(p, max_seconds: float, max_steps: int):
+    """FP64 CPU restatement (the oracle, faithful 7P+9 transforms) on all
+    host cores: returns (value, cores, sample description, steps, seconds)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np  # noqa: F401
+    import pf_ref  # the checker, used here only as the timed CPU baseline
+
+    cores = os.cpu_count() or 1
+    op = pf_ref.Params(p.Nx, p.Ny, p.Nz, p.var, t_step=p.t_step, grad_coeff_phi=p.grad_coeff_phi,
+                       grad_coeff_c=p.grad_coeff_c, D_S=p.D_S, D_L=p.D_L, D_gb=p.D_gb, mob_phi=p.mob_phi,
+                       sigma_1=p.sigma_1, sigma_2=p.sigma_2, am=p.am, ap=p.ap, con_0_mat=p.con_0_mat,
+                       con_0_ppt=p.con_0_ppt, mobility=p.mobility)
+    phi, con = pf_ref.ic_voronoi(op, IC["seed"], IC["n_grains"], IC["amp_phi"], IC["c0"], IC["amp_c"])
+    o = pf_ref.Oracle(op, phi, con, faithful=True, workers=cores)
+    o.step()  # warm-up (plans, page faults)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps:
+        o.step()
+        n += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    cells = p.Nx * p.Ny * p.Nz
+    value = cells * p.var * n / dt
+    sample = (f"{n} step(s) of the {p.Nx}^3 x {p.var} workload after 1 warm-up step, FP64, "
+              f"scipy.fft with {cores} workers, {7 * p.var + 9} 3-D transforms per step")
+    return value, cores, sample, n, dt
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU implementation of the path on the host cores
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    p = params()
+    budget = 150.0
+    value, cores, sample, n, dt = cpu_port_throughput(p, budget, max(1, args.steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-steps/s x P", "n_gpus": ws,
+        "steps": n, "warmup": 1, "ms_per_step": 1000.0 * dt / n, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Voronoi polycrystal, ran_2 stream)",
+        "config": {"workload": WORKLOAD_NAME, "grid": [p.Nx, p.Ny, p.Nz], "P": p.var,
+                   "sample": f"bounded to ~{budget:.0f} s of CPU time"},
+        "cpu_baseline": {"value": value, "unit": "cell-steps/s x P", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "cell-steps/s x P", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference's Fortran/MPI/P3DFFT build is not available on this host (no Fortran compiler, "
+                 "MPI, FFTW or P3DFFT); its FP64 algorithm is timed through the CPU restatement"),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    sys.path.insert(0, str(ROOT))
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    lib = pkg.load_library()
+    p = params()
+    cells = p.Nx * p.Ny * p.Nz
+    nF = p.var + 1
+    Kx = p.Nx // 2 + 1
+    var_mob = p.mobility == "c1mc" or p.D_gb != 0.0
+
+    phi_aos, con = pkg.ic_voronoi_aos(p, IC["seed"] + rank, IC["n_grains"], IC["amp_phi"], IC["c0"], IC["amp_c"],
+                                      pinned=True)
+    run = pkg.Run(p, device=local)
+    run.set_fields_aos(phi_aos, con)
+    b = run.batch_handle()
+    ext = torch.cuda.ExternalStream(lib.pf_batch_stream(b), device=local)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up
+    lib.pf_batch_enqueue(b, args.warmup)
+    torch.cuda.synchronize()
+
+    # timed region: K steps on the library's stream
+    clocks = Clocks(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(ext)
+    rc = lib.pf_batch_enqueue(b, args.steps)
+    ev1.record(ext)
+    ev1.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if rc != 0:
+        raise RuntimeError(lib.pf_last_error().decode())
+    # confirm the run stayed finite (one more step, untimed, with its record)
+    d = run.step(1)[0]
+    if d["nonfinite"]:
+        raise RuntimeError("non-finite values in the benchmark run")
+    if dist is not None:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cells * p.var * args.steps * ws / (ms / 1000.0)
+
+    # per-kernel timing on the same stream (each kernel alone, back to back)
+    plane = p.Ny * p.Nz * Kx * 8  # bytes of one field's half spectrum (complex64)
+    kernels = {
+        "x_pass": dict(phase=0, bytes=2 * nF * plane + (cells * 4 if var_mob else 0)),
+        # reads D~ and u_hat, writes u_hat and u~ (the c plane writes J~ instead of u~ under M(c))
+        "yz_pass": dict(phase=1, bytes=4 * nF * plane),
+    }
+    reps = max(20, min(200, args.steps // 4))
+    for name, k in kernels.items():
+        lib.pf_batch_enqueue_phase(b, k["phase"])
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(reps):
+            lib.pf_batch_enqueue_phase(b, k["phase"])
+        e1.record(ext)
+        e1.synchronize()
+        k["ms"] = e0.elapsed_time(e1) / reps
+    dom_name = max(kernels, key=lambda n: kernels[n]["ms"])
+    dom = kernels[dom_name]
+    peak, peak_kind = measured_hbm()
+    achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
+    traffic = ncu_traffic(dom_name)
+
+    # end to end through the C ABI with host buffers: upload the start fields
+    # from pinned memory, K steps with their diagnostic records returned to the
+    # host, download the fields (one output interval of K steps)
+    out_phi = torch.empty(phi_aos.shape, dtype=torch.float64, pin_memory=True).numpy()
+    out_con = torch.empty(con.shape, dtype=torch.float64, pin_memory=True).numpy()
+    run.set_fields_aos(phi_aos, con)
+    run.step(2)
+    barrier()
+    t0 = time.perf_counter()
+    run.set_fields_aos(phi_aos, con)
+    recs = run.step(args.steps)
+    run.get_fields_aos(out_phi, out_con)
+    t1 = time.perf_counter()
+    e2e_s = t1 - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = cells * p.var * args.steps * ws / e2e_s
+    field_bytes = (phi_aos.nbytes + con.nbytes)
+    diag_bytes = 80  # sizeof(pf_diag)
+    assert len(recs) == args.steps
+
+    kernels_per_step = 5 if var_mob else 3
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s x P", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Voronoi polycrystal from the ran_2 stream, no dataset)",
+            "config": {"workload": WORKLOAD_NAME, "grid": [p.Nx, p.Ny, p.Nz], "P": p.var, "runs_per_gpu": 1,
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single run",
+                       "l2": "inputs larger than L2: %.0f MB resident state + scratch per step > 129 MB L2" %
+                             ((3 * nF * plane + cells * 4 + plane) / 1e6)},
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": dom["bytes"], "ms_per_launch": dom["ms"],
+                         "other_kernels": {n: {"ms_per_launch": k["ms"], "algorithmic_bytes": k["bytes"],
+                                               "GB_s": k["bytes"] / (k["ms"] / 1000.0) / 1e9}
+                                           for n, k in kernels.items()}},
+            "clocks": clk,
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s x P",
+                    "h2d_bytes_per_step": field_bytes / args.steps,
+                    "d2h_bytes_per_step": field_bytes / args.steps + diag_bytes,
+                    "what": f"pf_set_fields (pinned host) + pf_step({args.steps}) with per-step records + "
+                            "pf_get_fields, host wall clock"},
+            "gpu_launches": kernels_per_step * args.steps,
+        }
+        if not args.no_cpu_baseline and ws == 1:
+            v, cores, sample, n, dt = cpu_port_throughput(p, 20.0, 50)
+            line["cpu_baseline"] = {"value": v, "unit": "cell-steps/s x P", "cores": cores, "kind": "port",
+                                    "sample": sample}
+        print(json.dumps(line), flush=True)
+    run.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

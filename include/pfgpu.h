@@ -147,6 +147,15 @@ typedef struct pf_ran2_state {
 void pf_ran2_init(pf_ran2_state* st);
 double pf_ran2(pf_ran2_state* st, int* idum);
 
+/* Seeded starts (host only).  Draw order z, y, x (x fastest), per cell var phi
+ * values then c, U(-a, a) = a (2 r - 1), r from ran_2 with idum = -(seed+1).
+ * pf_ic_voronoi first draws n_grains points (Nx r, Ny r, Nz r); every cell
+ * takes the nearest point (periodic minimum image, ties to the lower index)
+ * and grain s sets variant (s mod var) to 1 before the noise is added. */
+int pf_ic_noise(const pf_config* c, int seed, double amp_phi, double c0, double amp_c, double* phi_aos, double* con);
+int pf_ic_voronoi(const pf_config* c, int seed, int n_grains, double amp_phi, double c0, double amp_c,
+                  double* phi_aos, double* con);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,6 +9,7 @@ missing.
 """
 from . import build as build_mod
 from .pfgpu import (Batch, Config, Diag, PFError, Ran2, Run, load_library, library_path, make_config,
+                    ic_noise, ic_voronoi, ic_noise_aos, ic_voronoi_aos, to_aos, from_aos,
                     PF_FP32_FUSED, PF_FP64_PLAIN, PF_MOB_C1MC, PF_MOB_REFERENCE, EXPORTED)
 
 

@@ -44,52 +44,57 @@ static int fail(int code, const char* fmt, ...) {
 // One block per run, fixed summation order: results do not depend on how many
 // other runs share the launch.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) reduce_diag_kernel(const RunParams* __restrict__ runs, const Shape sh) {
+__global__ void __launch_bounds__(1024) reduce_diag_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   const RunParams& rp = runs[blockIdx.x];
-  __shared__ double sd[5][256];
-  __shared__ float sf[4][256];
-  const int t = threadIdx.x;
+  constexpr int NT = 1024;
+  __shared__ double sd[5][NT / 32];
+  __shared__ float sf[4][NT / 32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   double a_eta = 0, a_ch = 0, a_mass = 0, a_int = 0, a_bad = 0;
   float cmin = 1.f, cmax = 0.f, pmin = 1.f, ppmax = 0.f;
   const int nb = sh.nblk_x;
-  for (int i = t; i < nb; i += blockDim.x) {
-    a_eta += rp.part_x[XD_FETA * nb + i];
-    a_ch += rp.part_x[XD_FCH * nb + i];
-    a_mass += rp.part_x[XD_MASS * nb + i];
-    cmin = fminf(cmin, (float)rp.part_x[XD_CMIN * nb + i]);
-    cmax = fmaxf(cmax, (float)rp.part_x[XD_CMAX * nb + i]);
-    pmin = fminf(pmin, (float)rp.part_x[XD_PHIMIN * nb + i]);
-    ppmax = fmaxf(ppmax, (float)rp.part_x[XD_PHIPMAX * nb + i]);
-    a_bad += rp.part_x[XD_NONFINITE * nb + i];
+  const double* px = rp.part_x;
+#pragma unroll 4
+  for (int i = t; i < nb; i += NT) {
+    a_eta += px[XD_FETA * nb + i];
+    a_ch += px[XD_FCH * nb + i];
+    a_mass += px[XD_MASS * nb + i];
+    cmin = fminf(cmin, (float)px[XD_CMIN * nb + i]);
+    cmax = fmaxf(cmax, (float)px[XD_CMAX * nb + i]);
+    pmin = fminf(pmin, (float)px[XD_PHIMIN * nb + i]);
+    ppmax = fmaxf(ppmax, (float)px[XD_PHIPMAX * nb + i]);
+    a_bad += px[XD_NONFINITE * nb + i];
   }
-  for (int i = t; i < sh.nblk_yz; i += blockDim.x) a_int += rp.part_yz[i];
-  sd[0][t] = a_eta; sd[1][t] = a_ch; sd[2][t] = a_mass; sd[3][t] = a_int; sd[4][t] = a_bad;
-  sf[0][t] = cmin; sf[1][t] = cmax; sf[2][t] = pmin; sf[3][t] = ppmax;
+#pragma unroll 4
+  for (int i = t; i < sh.nblk_yz; i += NT) a_int += rp.part_yz[i];
+  a_eta = warp_sum(a_eta); a_ch = warp_sum(a_ch); a_mass = warp_sum(a_mass);
+  a_int = warp_sum(a_int); a_bad = warp_sum(a_bad);
+  cmin = warp_min(cmin); cmax = warp_max(cmax); pmin = warp_min(pmin); ppmax = warp_max(ppmax);
+  if (lane == 0) {
+    sd[0][w] = a_eta; sd[1][w] = a_ch; sd[2][w] = a_mass; sd[3][w] = a_int; sd[4][w] = a_bad;
+    sf[0][w] = cmin; sf[1][w] = cmax; sf[2][w] = pmin; sf[3][w] = ppmax;
+  }
   __syncthreads();
-  for (int s = 128; s > 0; s >>= 1) {
-    if (t < s) {
-#pragma unroll
-      for (int q = 0; q < 5; ++q) sd[q][t] += sd[q][t + s];
-      sf[0][t] = fminf(sf[0][t], sf[0][t + s]);
-      sf[1][t] = fmaxf(sf[1][t], sf[1][t + s]);
-      sf[2][t] = fminf(sf[2][t], sf[2][t + s]);
-      sf[3][t] = fmaxf(sf[3][t], sf[3][t + s]);
-    }
-    __syncthreads();
-  }
   if (t == 0) {
+    double s[5] = {0, 0, 0, 0, 0};
+    float m[4] = {1.f, 0.f, 1.f, 0.f};
+    for (int k = 0; k < NT / 32; ++k) {
+      for (int q = 0; q < 5; ++q) s[q] += sd[q][k];
+      m[0] = fminf(m[0], sf[0][k]); m[1] = fmaxf(m[1], sf[1][k]);
+      m[2] = fminf(m[2], sf[2][k]); m[3] = fmaxf(m[3], sf[3][k]);
+    }
     const int step = *rp.counter;
     double* d = rp.diag + (size_t)(step % rp.ring) * DR_COUNT;
     d[DR_STEP] = step + 1;
-    d[DR_FINT] = sd[3][0];
-    d[DR_FETA] = sd[0][0];
-    d[DR_FCH] = sd[1][0];
-    d[DR_CMIN] = sf[0][0];
-    d[DR_CMAX] = sf[1][0];
-    d[DR_PHIMIN] = sf[2][0];
-    d[DR_PHIPMAX] = sf[3][0];
-    d[DR_MASS] = sd[2][0];
-    d[DR_NONFINITE] = sd[4][0];
+    d[DR_FINT] = s[3];
+    d[DR_FETA] = s[0];
+    d[DR_FCH] = s[1];
+    d[DR_CMIN] = m[0];
+    d[DR_CMAX] = m[1];
+    d[DR_PHIMIN] = m[2];
+    d[DR_PHIPMAX] = m[3];
+    d[DR_MASS] = s[2];
+    d[DR_NONFINITE] = s[4];
     *rp.counter = step + 1;
   }
 }
@@ -249,30 +254,38 @@ struct pf_run {
   pf::Plain64* p64 = nullptr;
 };
 
-static int enqueue_step(pf_batch* b, cudaStream_t s) {
-  const Shape sh = b->tab.sh;
-  const int R = b->nruns;
-  const dim3 gx(b->Nz * (b->Ny / b->xk.wy), R);
-  b->xk.bulk<<<gx, 256, b->smem_x, s>>>(b->drp, sh);
+// One cluster launch of a yz-pass kernel over `planes` (field, kx) planes of
+// `nruns` runs starting at `runs`.
+static int launch_yz(pf_batch* b, KernelFn fn, int planes, const RunParams* runs, int nruns, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = b->yk.cluster;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
-  cfg.gridDim = dim3(b->yk.cluster * b->nF * b->Kx, R);
+  cfg.gridDim = dim3(b->yk.cluster * planes, nruns);
   cfg.blockDim = dim3(b->yk.threads);
   cfg.dynamicSmemBytes = b->yk.smem;
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  PF_CUDA(cudaLaunchKernelEx(&cfg, b->yk.main, (const RunParams*)b->drp, sh));
+  PF_CUDA(cudaLaunchKernelEx(&cfg, fn, runs, b->tab.sh));
+  return PF_OK;
+}
+
+static int enqueue_step(pf_batch* b, cudaStream_t s) {
+  const Shape sh = b->tab.sh;
+  const int R = b->nruns;
+  const dim3 gx(b->Nz * (b->Ny / b->xk.wy), R);
+  b->xk.bulk<<<gx, 256, b->smem_x, s>>>(b->drp, sh);
+  int rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, R, s);
+  if (rc) return rc;
   if (b->mob != MOB_CONST) {
     b->xk.xj<<<gx, 256, b->smem_xj, s>>>(b->drp, sh);
-    cfg.gridDim = dim3(b->yk.cluster * b->Kx, R);
-    PF_CUDA(cudaLaunchKernelEx(&cfg, b->yk.c2, (const RunParams*)b->drp, sh));
+    rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, s);
+    if (rc) return rc;
   }
-  reduce_diag_kernel<<<R, 256, 0, s>>>(b->drp, sh);
+  reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
   PF_CUDA(cudaGetLastError());
   return PF_OK;
 }
@@ -331,7 +344,7 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
     e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem_x);
     if (e != cudaSuccess) return bail(fail(PF_ECUDA, "x-pass smem attribute: %s", cudaGetErrorString(e)));
   }
-  for (KernelFn k : {b->yk.main, b->yk.c2}) {
+  for (KernelFn k : {b->yk.main, b->yk.c2, b->yk.imp}) {
     e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->yk.smem);
     if (e != cudaSuccess) return bail(fail(PF_ECUDA, "yz-pass smem attribute: %s", cudaGetErrorString(e)));
     if (b->yk.cluster > 8) {
@@ -368,12 +381,12 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const size_t szS = align(b->nF * fieldc * sizeof(float2));
   const size_t szMob = var ? align(ncell * sizeof(float)) : 0;
-  const size_t szJ = var ? align(fieldc * sizeof(float2)) : 0;
+  const size_t szJ = var ? align(fieldc * sizeof(float2)) : 0;  // J~ scratch
   const size_t szPx = align((size_t)XD_COUNT * sh.nblk_x * sizeof(double));
   const size_t szPyz = align((size_t)sh.nblk_yz * sizeof(double));
   const size_t szDiag = align((size_t)b->ring * DR_COUNT * sizeof(double));
   const size_t szCnt = 256;
-  const size_t per_run = 2 * szS + szMob + 2 * szJ + szPx + szPyz + szDiag + szCnt;
+  const size_t per_run = 3 * szS + szMob + szJ + szPx + szPyz + szDiag + szCnt;
   e = cudaMalloc(&b->mem, per_run * nruns);
   if (e != cudaSuccess)
     return bail(fail(PF_ENOMEM, "cudaMalloc(%zu bytes) for %d runs: %s", per_run * nruns, nruns, cudaGetErrorString(e)));
@@ -390,11 +403,11 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
     char* p = (char*)b->mem + per_run * i;
     RunParams& r = b->hrp[i];
     memset(&r, 0, sizeof r);
-    r.S = (float2*)p; p += szS;
+    r.Sk = (float2*)p; p += szS;
+    r.Sm = (float2*)p; p += szS;
     r.D = (float2*)p; p += szS;
     r.mob = var ? (float*)p : nullptr; p += szMob;
     r.J = var ? (float2*)p : nullptr; p += szJ;
-    r.A = var ? (float2*)p : nullptr; p += szJ;
     r.part_x = (double*)p; p += szPx;
     r.part_yz = (double*)p; p += szPyz;
     r.diag = (double*)p; p += szDiag;
@@ -449,6 +462,8 @@ static int batch_set_fields(pf_batch* b, int run, const double* phi, const doubl
   aos_to_soa_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, b->stream>>>(dphi, dcon, b->fin, b->V, ncell);
   const dim3 gx(b->Nz * (b->Ny / b->xk.wy), 1);
   b->xk.imp<<<gx, 256, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
+  int rc = launch_yz(b, b->yk.imp, b->nF * b->Kx, b->drp + run, 1, b->stream);
+  if (rc) return rc;
   PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, sizeof(int), b->stream));
   PF_CUDA(cudaGetLastError());
   PF_CUDA(cudaStreamSynchronize(b->stream));
@@ -497,8 +512,14 @@ static int batch_step(pf_batch* b, int nsteps, pf_diag* diag) {
     PF_CUDA(cudaStreamSynchronize(b->stream));
     b->hdiag.resize((size_t)b->ring * DR_COUNT);
     for (int r = 0; r < b->nruns; ++r) {
-      PF_CUDA(cudaMemcpy(b->hdiag.data(), b->hrp[r].diag, (size_t)b->ring * DR_COUNT * sizeof(double),
-                         cudaMemcpyDeviceToHost));
+      // copy only this chunk's records (two pieces when they wrap around the ring)
+      const int first = b->steps_done[r] % b->ring;
+      const int n1 = std::min(chunk, b->ring - first);
+      PF_CUDA(cudaMemcpy(b->hdiag.data() + (size_t)first * DR_COUNT, b->hrp[r].diag + (size_t)first * DR_COUNT,
+                         (size_t)n1 * DR_COUNT * sizeof(double), cudaMemcpyDeviceToHost));
+      if (chunk > n1)
+        PF_CUDA(cudaMemcpy(b->hdiag.data(), b->hrp[r].diag, (size_t)(chunk - n1) * DR_COUNT * sizeof(double),
+                           cudaMemcpyDeviceToHost));
       for (int s = 0; s < chunk; ++s) {
         const int step = b->steps_done[r] + s;  // 0-based
         const double* d = b->hdiag.data() + (size_t)(step % b->ring) * DR_COUNT;
@@ -610,19 +631,8 @@ int pf_batch_enqueue_phase(pf_batch* b, int phase) {
   if (phase == 0) {
     b->xk.bulk<<<gx, 256, b->smem_x, b->stream>>>(b->drp, sh);
   } else {
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = b->yk.cluster;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(b->yk.cluster * b->nF * b->Kx, b->nruns);
-    cfg.blockDim = dim3(b->yk.threads);
-    cfg.dynamicSmemBytes = b->yk.smem;
-    cfg.stream = b->stream;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    PF_CUDA(cudaLaunchKernelEx(&cfg, b->yk.main, (const RunParams*)b->drp, sh));
+    int rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, b->nruns, b->stream);
+    if (rc) return rc;
   }
   PF_CUDA(cudaGetLastError());
   return PF_OK;

@@ -212,6 +212,61 @@ struct Line {
   __device__ __forceinline__ static int pos_of_freq(int k) { return k / N2 + N1 * (k % N2); }
 };
 
+// ---------------------------------------------------------------------------
+// Single passes (no barrier inside), over `nb` (1 or 2) buffers of `nl` lines
+// each: line l of buffer b starts at (b ? b1 : b0) + l*pitch.
+// ---------------------------------------------------------------------------
+template <int L>
+__device__ __forceinline__ void pass_a_fwd(float2* b0, float2* b1, int nb, int nl, int pitch, const float2* __restrict__ tw) {
+  constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
+  const int tot = nb * nl * N1;
+  for (int it = threadIdx.x; it < tot; it += blockDim.x) {
+    const int n1 = it % N1, r = it / N1, l = r % nl, b = r / nl;
+    float2* p = (b ? b1 : b0) + l * pitch + n1;
+    float2 v[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) v[n2] = p[n2 * (N1 + 1)];
+    Dft<N2>::fwd(v);
+#pragma unroll
+    for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], __ldg(tw + n1 * k2));
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) p[k2 * (N1 + 1)] = v[k2];
+  }
+}
+
+template <int L, bool INV>
+__device__ __forceinline__ void pass_b(float2* b0, float2* b1, int nb, int nl, int pitch) {
+  constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
+  const int tot = nb * nl * N2;
+  for (int it = threadIdx.x; it < tot; it += blockDim.x) {
+    const int k2 = it % N2, r = it / N2, l = r % nl, b = r / nl;
+    float2* p = (b ? b1 : b0) + l * pitch + k2 * (N1 + 1);
+    float2 u[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) u[n1] = p[n1];
+    if (INV) dft_inv<N1>(u); else Dft<N1>::fwd(u);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) p[k1] = u[k1];
+  }
+}
+
+template <int L>
+__device__ __forceinline__ void pass_a_inv(float2* b0, float2* b1, int nb, int nl, int pitch, const float2* __restrict__ tw) {
+  constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
+  const int tot = nb * nl * N1;
+  for (int it = threadIdx.x; it < tot; it += blockDim.x) {
+    const int n1 = it % N1, r = it / N1, l = r % nl, b = r / nl;
+    float2* p = (b ? b1 : b0) + l * pitch + n1;
+    float2 v[N2];
+    v[0] = p[0];
+#pragma unroll
+    for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * (N1 + 1)], __ldg(tw + n1 * k2));
+    dft_inv<N2>(v);
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) p[n2 * (N1 + 1)] = v[n2];
+  }
+}
+
 // Forward transform of `nlines` lines of length L stored at buf + l*pitch
 // (phys() layout inside each line).  tw = W_L^j, j in [0, L), from a table.
 // Must be called by all threads of the block; ends with __syncthreads().

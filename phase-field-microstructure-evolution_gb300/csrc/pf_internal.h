@@ -16,7 +16,7 @@ struct XKernels {
 };
 
 struct YZKernels {
-  KernelFn main, c2;
+  KernelFn main, c2, imp;  // modes YZ_MAIN, YZ_C2, YZ_IMPORT
   int cluster;   // CTAs per plane
   int threads;   // threads per CTA
   size_t smem;   // dynamic shared memory per CTA

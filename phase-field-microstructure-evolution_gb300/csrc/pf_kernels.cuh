@@ -1,25 +1,29 @@
 // Fused FP32 kernels of the semi-implicit spectral step (sm_103a).
 //
-// State of one run ("mixed" representation): for every field f (the var order
-// parameters, then the concentration c) the x-direction half spectrum
-//     S[f][kx][z][y] = (1/Nx) sum_x u_f(x,y,z) e^{-2 pi i kx x / Nx},  kx = 0..Nx/2
-// (float2, y fastest).  The reference keeps phi/con in real space and takes a
-// full 3-D R2C per field (src/f_trans.f90:11-12); here the x transform of the
-// state is kept, so one step costs exactly two passes over the fields:
+// State of one run, for every field f (the var order parameters, then the
+// concentration c):
+//   Sk[f][kx][ypos][zpos]  u_hat in k-space (normalised like f_trans,
+//                          src/f_trans.f90:12), y/z in digit-transposed order;
+//   Sm[f][kx][z][y]        the same field in "mixed" space: its x half
+//                          spectrum (1/Nx) sum_x u e^{-2 pi i kx x/Nx} with y, z
+//                          in real space (what the x pass needs).
+// The reference keeps phi/con in real space and takes a full 3-D R2C per
+// field and use (src/f_trans.f90:11-12, 7*var+9 transforms per step); here one
+// step is two passes over the fields:
 //
 //   x pass  (x_pass_kernel, one CTA per WY y-rows at one z, all fields):
-//       S --C2R_x--> phi, c --bulk terms (src/var_diff.f90:685-898)-->
+//       Sm --C2R_x--> phi, c --bulk terms (src/var_diff.f90:685-898)-->
 //       dF/dphi_i, dF/dc (, mobility) --R2C_x/Nx--> D
 //   yz pass (yz_kernel, one CTA cluster per (field, kx) plane):
-//       DFT_yz(S), DFT_yz(D) --semi-implicit increment--> IDFT_yz --> S += increment
+//       D --DFT_yz--> D_hat;  u_hat += m1 u_hat + m2 D_hat  (pointwise);
+//       u_hat --IDFT_yz--> Sm
 //
-// The update is applied as an increment, delta_hat = m1 * u_hat + m2 * D_hat,
-// so that the O(1) state never takes an FP32 round trip through the FFT; only
-// the small increment does.  In exact arithmetic
-//   u_hat + delta_hat = (u_hat - L dt D_hat) / (1 - L kappa dt K2)      (AC, :1020-1024)
-//   c_hat + delta_hat = (c_hat + D_mean K2 dt mu_hat) / (1 + D_mean dt kappa_c K4)   (CH, :976-983)
-// with the variable-mobility term dt G J'_hat / (...) of :976-983 added by a
-// second x/yz pass pair (xj pass + yz_kernel in C2 mode).
+// In exact arithmetic the pointwise update is the reference's
+//   u_hat_new = (u_hat - L dt D_hat) / (1 - L kappa dt K2)                (AC, :1020-1024)
+//   c_hat_new = (c_hat + D_mean K2 dt mu_hat) / (1 + D_mean dt kappa_c K4)  (CH, :976-983)
+// written as an increment so that the state never takes an FP32 round trip
+// through an FFT.  The variable-mobility term dt G J'_hat / (...) of :976-983 is
+// added by a second x/yz pass pair (xj pass + yz_kernel in C2 mode).
 #pragma once
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
@@ -42,11 +46,11 @@ enum Mobility { MOB_CONST = 0, MOB_REF_VAR = 1, MOB_C1MC = 2 };
 
 // Device-side description of one run (all runs of a launch share one shape)
 struct RunParams {
-  float2* S;       // [nF][Kx][Nz][Ny] state
+  float2* Sk;      // [nF][Kx][Ny][Nz] state in k-space (digit-transposed y, z positions)
+  float2* Sm;      // [nF][Kx][Nz][Ny] state in mixed space (x spectrum, real-space y, z)
   float2* D;       // [nF][Kx][Nz][Ny] x-spectra of dF/dphi_i and dF/dc
   float* mob;      // [Nz][Ny][Nx] mobility minus D_mean (variable mobility only)
   float2* J;       // [Kx][Nz][Ny] CH flux scratch (variable mobility only)
-  float2* A;       // [Kx][Nz][Ny] constant-mobility part of the c increment (idem)
   double* part_x;  // [XD_COUNT][nblk_x]
   double* part_yz; // [nblk_yz]
   double* diag;    // [ring][DR_COUNT]
@@ -153,7 +157,7 @@ __device__ __forceinline__ void r2c_post(const float2* line, int k, float scale,
 // component of the float2 slot, i.e. cell x = 2m + sel.
 // ---------------------------------------------------------------------------
 struct BulkAcc {
-  double feta, fch, mass;
+  float feta, fch, mass;  // per-thread partial sums over a few cells (FP64 from the warp level up)
   float cmin, cmax, phimin, phipmax;
   int nonfinite;
 };
@@ -220,10 +224,10 @@ __device__ __forceinline__ void bulk_cell(float2* smem, int yy, int slot, int se
   const float dcm = c - rp.c0m, dcp = c - rp.c0p;
   const float fm = rp.am * dcm * dcm, fp = rp.ap * dcp * dcp;
   const float dfm = fm - fp;
-  acc.fch += (double)(h * fm + (1.f - h) * fp);
+  acc.fch += h * fm + (1.f - h) * fp;
   dfdc_out = 2.f * h * rp.am * dcm + 2.f * (1.f - h) * rp.ap * dcp;
-  acc.feta += (double)(-0.5f * S2 + 0.25f * S4 + sg1 * pairs + sg2 * pP2 * Smat);
-  acc.mass += (double)c;
+  acc.feta += -0.5f * S2 + 0.25f * S4 + sg1 * pairs + sg2 * pP2 * Smat;
+  acc.mass += c;
   acc.cmin = fminf(acc.cmin, c);
   acc.cmax = fmaxf(acc.cmax, c);
   acc.phimin = fminf(acc.phimin, S2);
@@ -282,7 +286,7 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
   const size_t plane = (size_t)sh.Nz * sh.Ny;
   const size_t fstride = (size_t)sh.Kx * plane;
   const size_t row_off = (size_t)z * sh.Ny + y0;
-  const float2* __restrict__ src = (MODE == MODE_XJ) ? rp.J : rp.S;
+  const float2* __restrict__ src = (MODE == MODE_XJ) ? rp.J : rp.Sm;
 
   if (MODE == MODE_IMPORT) {
     // real rows -> interleaved lines (natural order)
@@ -316,7 +320,7 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
   }
 
   BulkAcc acc;
-  acc.feta = 0.0; acc.fch = 0.0; acc.mass = 0.0;
+  acc.feta = 0.f; acc.fch = 0.f; acc.mass = 0.f;
   acc.cmin = 1.0f; acc.cmax = 0.0f; acc.phimin = 1.0f; acc.phipmax = 0.0f;  // reference start values
   acc.nonfinite = 0;
 
@@ -348,7 +352,7 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
 
   // 4. forward x transform and 5. R2C post-processing, scaled by 1/Nx
   fft_fwd_lines<M>(smem, nF * WY, PM, sh.twM);
-  float2* __restrict__ dst = (MODE == MODE_BULK) ? rp.D : (MODE == MODE_XJ ? rp.J : rp.S);
+  float2* __restrict__ dst = (MODE == MODE_BULK) ? rp.D : (MODE == MODE_XJ ? rp.J : rp.Sm);
   const float scale = 1.0f / (float)NX;
   for (int it = threadIdx.x; it < nF * WY * NPAIR; it += blockDim.x) {
     const int yy = it % WY, r = it / WY, k = r % NPAIR, f = r / NPAIR;
@@ -366,7 +370,7 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
   __shared__ float red_f[4][8];
   __shared__ int red_i[8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double s0 = warp_sum(acc.feta), s1 = warp_sum(acc.fch), s2 = warp_sum(acc.mass);
+  double s0 = warp_sum((double)acc.feta), s1 = warp_sum((double)acc.fch), s2 = warp_sum((double)acc.mass);
   float m0 = warp_min(acc.cmin), m1 = warp_max(acc.cmax), m2 = warp_min(acc.phimin), m3 = warp_max(acc.phipmax);
   int nb = __reduce_add_sync(0xffffffffu, acc.nonfinite);
   if (lane == 0) {
@@ -400,26 +404,33 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// yz pass: 2-D DFT over (y, z) of one kx plane, the spectral update, inverse.
-// A cluster of C CTAs shares one plane: CTA r holds z rows [r*NZ/C, ...) for the
-// y transforms ("A layout", lines along y) and y positions [r*NY/C, ...) for
-// the z transforms ("B layout", lines along z); the two layouts are exchanged
-// through distributed shared memory.
+// yz pass.  The state of every field is kept in full k-space,
+//     Sk[f][kx][ypos][zpos] = u_hat (normalised like f_trans, src/f_trans.f90:12),
+// in the digit-transposed position order of the y and z transforms, and is
+// updated pointwise there (exact increment, no FFT round trip of the state).
+// Per (field, kx) plane the yz pass
+//   * transforms D~ (the x pass output, mixed space) forward over y and z,
+//   * forms u_hat_new = u_hat + m1 u_hat + m2 D_hat (semi-implicit update),
+//   * transforms u_hat_new back over z and y to the mixed-space field the next
+//     x pass reads (Sm).
+// A cluster of C CTAs shares a plane: CTA r holds z rows [r*NZ/C, ...) for
+// the y transforms ("A layout") and y positions [r*NY/C, ...) for the z
+// transforms ("B layout"); the layouts are exchanged through distributed
+// shared memory.  All loops have compile-time trip counts.
 // ---------------------------------------------------------------------------
 template <int NY, int NZ, int C>
 struct YZ {
-  static constexpr int LA = NZ / C;
-  static constexpr int LB = NY / C;
+  static constexpr int LA = NZ / C;  // z rows per CTA (A layout)
+  static constexpr int LB = NY / C;  // y positions per CTA (B layout)
   static constexpr int PY = Line<NY>::PITCH;
   static constexpr int PZ = Line<NZ>::PITCH;
   static constexpr int UA = LA * PY;
   static constexpr int UB = LB * PZ;
-  static constexpr int U = (UA > UB ? UA : UB);
-  static constexpr size_t SMEM = 3 * (size_t)U * sizeof(float2);
+  static constexpr size_t SMEM = (size_t)(UA + UB) * sizeof(float2);
   static_assert(NZ % C == 0 && NY % C == 0, "cluster must divide the plane");
 };
 
-enum YZMode { YZ_MAIN = 0, YZ_C2 = 1 };
+enum YZMode { YZ_MAIN = 0, YZ_C2 = 1, YZ_IMPORT = 2 };
 
 template <int C>
 __device__ __forceinline__ void cluster_barrier() {
@@ -430,100 +441,155 @@ __device__ __forceinline__ void cluster_barrier() {
   }
 }
 
-// B[yl][phys_z(z)] <- A_{owner(z)}[z % LA][phys_y(r*LB + yl)]
-template <int NY, int NZ, int C>
-__device__ __forceinline__ void exch_AB(float2* __restrict__ dstB, float2* const* srcA, int r) {
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t map_rank(uint32_t a, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+template <int C>
+__device__ __forceinline__ float2 ld_peer(uint32_t a) {
+  float2 v;
+  if constexpr (C == 1) {
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  } else {
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  }
+  return v;
+}
+
+// B[yl][phys_z(z)] <- A_{owner(z)}[z % LA][phys_y(r*LB + yl)], consecutive
+// threads read consecutive y positions of one peer row.
+template <int NY, int NZ, int C, int T>
+__device__ __forceinline__ void exch_AB(float2* __restrict__ B, uint32_t A_base, int r) {
   using G = YZ<NY, NZ, C>;
   constexpr int TOTAL = G::LB * NZ;
-  constexpr int K = 4;
-  for (int base = threadIdx.x; base < TOTAL; base += blockDim.x * K) {
+  static_assert(T % G::LB == 0, "threads must cover whole rows");
+  constexpr int S = T / G::LB;  // z step per iteration
+  constexpr int ITER = (TOTAL + T - 1) / T;
+  const int yl = threadIdx.x % G::LB;
+  const int z0 = threadIdx.x / G::LB;
+  const uint32_t src_off = (uint32_t)(Line<NY>::phys(r * G::LB + yl)) * 8u;
+  constexpr int K = 8;
+#pragma unroll
+  for (int j0 = 0; j0 < ITER; j0 += K) {
     float2 v[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int i = base + k * blockDim.x;
-      if (i < TOTAL) {
-        const int yl = i % G::LB, z = i / G::LB;
+      const int z = z0 + (j0 + k) * S;
+      if (j0 + k < ITER && z < NZ) {
         const int owner = z / G::LA, zl = z - owner * G::LA;
-        v[k] = srcA[owner][zl * G::PY + Line<NY>::phys(r * G::LB + yl)];
+        const uint32_t a = A_base + (uint32_t)(zl * G::PY) * 8u + src_off;
+        v[k] = ld_peer<C>(C == 1 ? a : map_rank(a, owner));
       }
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int i = base + k * blockDim.x;
-      if (i < TOTAL) {
-        const int yl = i % G::LB, z = i / G::LB;
-        dstB[yl * G::PZ + Line<NZ>::phys(z)] = v[k];
-      }
+      const int z = z0 + (j0 + k) * S;
+      if (j0 + k < ITER && z < NZ) B[yl * G::PZ + Line<NZ>::phys(z)] = v[k];
     }
   }
 }
 
-// A[zl][phys_y(y)] <- B_{owner(y)}[y % LB][phys_z(r*LA + zl)]
-template <int NY, int NZ, int C>
-__device__ __forceinline__ void exch_BA(float2* __restrict__ dstA, float2* const* srcB, int r) {
+// A[zl][phys_y(y)] <- B_{owner(y)}[y % LB][phys_z(r*LA + zl)], consecutive
+// threads read consecutive z positions of one peer line.
+template <int NY, int NZ, int C, int T>
+__device__ __forceinline__ void exch_BA(float2* __restrict__ A, uint32_t B_base, int r) {
   using G = YZ<NY, NZ, C>;
   constexpr int TOTAL = G::LA * NY;
-  constexpr int K = 4;
-  for (int base = threadIdx.x; base < TOTAL; base += blockDim.x * K) {
+  static_assert(T % G::LA == 0, "threads must cover whole lines");
+  constexpr int S = T / G::LA;
+  constexpr int ITER = (TOTAL + T - 1) / T;
+  const int zl = threadIdx.x % G::LA;
+  const int y0 = threadIdx.x / G::LA;
+  const uint32_t src_off = (uint32_t)(Line<NZ>::phys(r * G::LA + zl)) * 8u;
+  constexpr int K = 8;
+#pragma unroll
+  for (int j0 = 0; j0 < ITER; j0 += K) {
     float2 v[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int i = base + k * blockDim.x;
-      if (i < TOTAL) {
-        const int zl = i % G::LA, y = i / G::LA;
+      const int y = y0 + (j0 + k) * S;
+      if (j0 + k < ITER && y < NY) {
         const int owner = y / G::LB, yl = y - owner * G::LB;
-        v[k] = srcB[owner][yl * G::PZ + Line<NZ>::phys(r * G::LA + zl)];
+        const uint32_t a = B_base + (uint32_t)(yl * G::PZ) * 8u + src_off;
+        v[k] = ld_peer<C>(C == 1 ? a : map_rank(a, owner));
       }
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int i = base + k * blockDim.x;
-      if (i < TOTAL) {
-        const int zl = i % G::LA, y = i / G::LA;
-        dstA[zl * G::PY + Line<NY>::phys(y)] = v[k];
-      }
+      const int y = y0 + (j0 + k) * S;
+      if (j0 + k < ITER && y < NY) A[zl * G::PY + Line<NY>::phys(y)] = v[k];
     }
   }
 }
 
-// global rows z in [z0, z0+LA) of a plane -> A layout
-template <int NY, int NZ, int C>
-__device__ __forceinline__ void load_rows(float2* __restrict__ dstA, const float2* __restrict__ plane, int z0) {
-  using G = YZ<NY, NZ, C>;
-  constexpr int TOTAL = G::LA * NY / 2;
-  constexpr int K = 4;
-  for (int base = threadIdx.x; base < TOTAL; base += blockDim.x * K) {
-    float4 v[K];
+// pass A (forward or inverse) over NL lines of length L, pitch P, T threads
+template <int L, int NL, int P, int T, bool INV>
+__device__ __forceinline__ void passA(float2* buf, const float2* __restrict__ tw) {
+  constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
+  static_assert(T % N1 == 0, "threads must be a multiple of N1");
+  const int n1 = threadIdx.x % N1;
+  float2 w[N2];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int i = base + k * blockDim.x;
-      if (i < TOTAL) {
-        const int y2 = i % (NY / 2), zl = i / (NY / 2);
-        v[k] = __ldg(reinterpret_cast<const float4*>(plane + (size_t)(z0 + zl) * NY) + y2);
-      }
+  for (int k2 = 1; k2 < N2; ++k2) w[k2] = __ldg(tw + n1 * k2);
+  constexpr int ITEMS = NL * N1, ITER = (ITEMS + T - 1) / T;
+#pragma unroll
+  for (int j = 0; j < ITER; ++j) {
+    const int it = threadIdx.x + j * T;
+    if (ITEMS % T != 0 && it >= ITEMS) break;
+    const int l = it / N1;
+    float2* p = buf + l * P + n1;
+    float2 v[N2];
+    if (!INV) {
+#pragma unroll
+      for (int n2 = 0; n2 < N2; ++n2) v[n2] = p[n2 * (N1 + 1)];
+      Dft<N2>::fwd(v);
+#pragma unroll
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], w[k2]);
+    } else {
+      v[0] = p[0];
+#pragma unroll
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * (N1 + 1)], w[k2]);
+      dft_inv<N2>(v);
     }
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int i = base + k * blockDim.x;
-      if (i < TOTAL) {
-        const int y2 = i % (NY / 2), zl = i / (NY / 2);
-        float2* d = dstA + zl * G::PY + Line<NY>::phys(2 * y2);
-        d[0] = make_float2(v[k].x, v[k].y);
-        d[1] = make_float2(v[k].z, v[k].w);  // 2*y2 and 2*y2+1 share a run (N1 even)
-      }
-    }
+    for (int k = 0; k < N2; ++k) p[k * (N1 + 1)] = v[k];
   }
 }
 
-template <int NY, int NZ, int C, int MODE>
-__global__ void __launch_bounds__(512) yz_kernel(const RunParams* __restrict__ runs, const Shape sh) {
+template <int L, int NL, int P, int T, bool INV>
+__device__ __forceinline__ void passB(float2* buf) {
+  constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
+  static_assert(T % N2 == 0, "threads must be a multiple of N2");
+  const int k2 = threadIdx.x % N2;
+  constexpr int ITEMS = NL * N2, ITER = (ITEMS + T - 1) / T;
+#pragma unroll
+  for (int j = 0; j < ITER; ++j) {
+    const int it = threadIdx.x + j * T;
+    if (ITEMS % T != 0 && it >= ITEMS) break;
+    const int l = it / N2;
+    float2* p = buf + l * P + k2 * (N1 + 1);
+    float2 u[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) u[n1] = p[n1];
+    if (INV) dft_inv<N1>(u); else Dft<N1>::fwd(u);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) p[k1] = u[k1];
+  }
+}
+
+template <int NY, int NZ, int C, int T, int MODE>
+__global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = YZ<NY, NZ, C>;
+  using LY = Line<NY>;
+  using LZ = Line<NZ>;
+  constexpr int N1y = LY::N1, N2y = LY::N2, N1z = LZ::N1, N2z = LZ::N2;
+  static_assert(T % N1y == 0 && T % N2z == 0, "thread count");
   extern __shared__ float2 smem[];
-  __shared__ float2* rU[3][C > 0 ? C : 1];
-  __shared__ double red[16];
-  float2* U0 = smem;
-  float2* U1 = smem + G::U;
-  float2* U2 = smem + 2 * G::U;
+  __shared__ double red[T / 32];
+  float2* UA = smem;
+  float2* UB = smem + G::UA;
   const RunParams& rp = runs[blockIdx.y];
   const int r = (C == 1) ? 0 : (int)(blockIdx.x % C);
   const int p = blockIdx.x / C;
@@ -532,159 +598,179 @@ __global__ void __launch_bounds__(512) yz_kernel(const RunParams* __restrict__ r
   const int kx = p - (p / Kx) * Kx;
   const size_t plane_elems = (size_t)NZ * NY;
   const size_t fstride = (size_t)Kx * plane_elems;
+  const size_t poff = f * fstride + kx * plane_elems;
   const bool is_c = (f == rp.V);
-  const bool var_c = is_c && rp.mobility != MOB_CONST;  // variable-mobility c plane
+  const bool var_c = (MODE == YZ_MAIN) && is_c && rp.mobility != MOB_CONST;
   const int z0 = r * G::LA;
 
-  if (threadIdx.x < C) {
-    if constexpr (C == 1) {
-      rU[0][0] = U0; rU[1][0] = U1; rU[2][0] = U2;
-    } else {
-      cg::cluster_group cl = cg::this_cluster();
-      rU[0][threadIdx.x] = cl.map_shared_rank(U0, threadIdx.x);
-      rU[1][threadIdx.x] = cl.map_shared_rank(U1, threadIdx.x);
-      rU[2][threadIdx.x] = cl.map_shared_rank(U2, threadIdx.x);
+  // 1. forward y transform of the mixed-space input rows z0..z0+LA
+  //    (MAIN/IMPORT: D~ or S~; C2: J~'), first pass straight from global
+  {
+    const float2* src = (MODE == YZ_MAIN) ? rp.D + poff : (MODE == YZ_C2 ? rp.J + kx * plane_elems : rp.Sm + poff);
+    const int n1 = threadIdx.x % N1y;
+    float2 w[N2y];
+#pragma unroll
+    for (int k2 = 1; k2 < N2y; ++k2) w[k2] = __ldg(sh.twY + n1 * k2);
+    constexpr int ITEMS = G::LA * N1y, ITER = (ITEMS + T - 1) / T;
+#pragma unroll
+    for (int j = 0; j < ITER; ++j) {
+      const int it = threadIdx.x + j * T;
+      if (ITEMS % T != 0 && it >= ITEMS) break;
+      const int zl = it / N1y;
+      const float2* s = src + (size_t)(z0 + zl) * NY + n1;
+      float2 v[N2y];
+#pragma unroll
+      for (int n2 = 0; n2 < N2y; ++n2) v[n2] = __ldg(s + n2 * N1y);
+      Dft<N2y>::fwd(v);
+      float2* d = UA + zl * G::PY + n1;
+      d[0] = v[0];
+#pragma unroll
+      for (int k2 = 1; k2 < N2y; ++k2) d[k2 * (N1y + 1)] = cmul(v[k2], w[k2]);
     }
   }
-
-  // 1. load rows (A layout): u -> U1, D -> U2   (C2 mode: J~' -> U1)
-  if (MODE == YZ_MAIN) {
-    load_rows<NY, NZ, C>(U1, rp.S + f * fstride + kx * plane_elems, z0);
-    load_rows<NY, NZ, C>(U2, rp.D + f * fstride + kx * plane_elems, z0);
-  } else {
-    load_rows<NY, NZ, C>(U1, rp.J + kx * plane_elems, z0);
-  }
   __syncthreads();
-  // 2. y transforms
-  fft_fwd_lines<NY>(U1, G::LA, G::PY, sh.twY);
-  if (MODE == YZ_MAIN) fft_fwd_lines<NY>(U2, G::LA, G::PY, sh.twY);
+  passB<NY, G::LA, G::PY, T, false>(UA);
   cluster_barrier<C>();
-  // 3. A -> B exchanges: u -> U0, D -> U1
-  exch_AB<NY, NZ, C>(U0, rU[1], r);
-  if (MODE == YZ_MAIN) {
-    cluster_barrier<C>();
-    exch_AB<NY, NZ, C>(U1, rU[2], r);
-  }
+  exch_AB<NY, NZ, C, T>(UB, smem_addr(UA), r);
   __syncthreads();
-  // 4. z transforms
-  fft_fwd_lines<NZ>(U0, G::LB, G::PZ, sh.twZ);
-  if (MODE == YZ_MAIN) fft_fwd_lines<NZ>(U1, G::LB, G::PZ, sh.twZ);
+  passA<NZ, G::LB, G::PZ, T, false>(UB, sh.twZ);
+  __syncthreads();
 
-  // 5. spectral update at every (ky, kz) held by this CTA
+  // 2. last forward z pass, pointwise k-space update, first inverse z pass,
+  //    fused per run of N1z positions
   const float inv_nyz = 1.0f / (float)(NY * NZ);
   const float qx2 = sh.qx2[kx], qx4 = sh.qx4[kx], qnx = sh.qnx[kx];
   const float wkx = (kx == 0 || 2 * kx == sh.Nx) ? 1.0f : 2.0f;
   float fint = 0.f;
-  for (int it = threadIdx.x; it < G::LB * NZ; it += blockDim.x) {
-    const int zp = it % NZ, yl = it / NZ;
-    const int ky = Line<NY>::freq_of_pos(r * G::LB + yl);
-    const int kz = Line<NZ>::freq_of_pos(zp);
-    const int a = yl * G::PZ + Line<NZ>::phys(zp);
-    const float q2 = qx2 + __ldg(sh.qy2 + ky) + __ldg(sh.qz2 + kz);
-    const float qn_y = __ldg(sh.qny + ky), qn_z = __ldg(sh.qnz + kz);
-    if (MODE == YZ_MAIN) {
-      const float2 u = U0[a];
-      const float2 d = U1[a];
-      const float kn2 = qnx * qnx + qn_y * qn_y + qn_z * qn_z;
-      fint = fmaf(kn2, u.x * u.x + u.y * u.y, fint);
-      if (!is_c) {
-        // AC, :1015-1024.  den = 1 + L kappa dt q^2
-        const float lk = rp.L * rp.dt;
-        const float den = fmaf(lk * rp.kappa_phi, q2, 1.0f);
-        const float inv = inv_nyz / den;
-        const float m1 = -lk * rp.kappa_phi * q2 * inv;
-        const float m2 = -lk * inv;
-        U0[a] = make_float2(fmaf(m1, u.x, m2 * d.x), fmaf(m1, u.y, m2 * d.y));
-      } else {
-        // CH, :976-983.  den = 1 + D dt kappa_c K4,  K2 = -q^2
-        const float q4 = qx4 + __ldg(sh.qy4 + ky) + __ldg(sh.qz4 + kz);
-        const float dd = rp.D_L * rp.dt;
-        const float den = fmaf(dd * rp.kappa_c, q4, 1.0f);
-        const float inv = inv_nyz / den;
-        const float m1 = -dd * rp.kappa_c * q4 * inv;
-        const float m2 = -dd * q2 * inv;
-        U0[a] = make_float2(fmaf(m1, u.x, m2 * d.x), fmaf(m1, u.y, m2 * d.y));
-        if (var_c) {
-          // J_hat = G mu_hat - kappa_c c_hat K3 (:932-935), G = i*g, K3 = i*k3
-          const float g = qnx + qn_y + qn_z;
-          const float k3 = -(qnx * qx2 + qn_y * __ldg(sh.qy2 + ky) + qn_z * __ldg(sh.qz2 + kz));
-          // i*(g*d - kappa_c*k3*u) * inv_nyz
-          const float2 t = make_float2((g * d.x - rp.kappa_c * k3 * u.x) * inv_nyz,
-                                       (g * d.y - rp.kappa_c * k3 * u.y) * inv_nyz);
-          U1[a] = cmul_pi(t);
+  {
+    const int k2 = threadIdx.x % N2z;
+    constexpr int ITEMS = G::LB * N2z, ITER = (ITEMS + T - 1) / T;
+#pragma unroll 1
+    for (int j = 0; j < ITER; ++j) {
+      const int it = threadIdx.x + j * T;
+      if (ITEMS % T != 0 && it >= ITEMS) break;
+      const int yl = it / N2z;
+      const int ypos = r * G::LB + yl;
+      const int ky = LY::freq_of_pos(ypos);
+      const float qy2 = __ldg(sh.qy2 + ky), qy4 = __ldg(sh.qy4 + ky), qn_y = __ldg(sh.qny + ky);
+      float2* pb = UB + yl * G::PZ + k2 * (N1z + 1);
+      float2* gk = rp.Sk + poff + (size_t)ypos * NZ + k2 * N1z;  // k-space state run
+      float2 d[N1z], u[N1z];
+#pragma unroll
+      for (int k1 = 0; k1 < N1z; ++k1) d[k1] = pb[k1];
+      Dft<N1z>::fwd(d);
+      if (MODE != YZ_IMPORT) {
+#pragma unroll
+        for (int k1 = 0; k1 < N1z; k1 += 2) {
+          const float4 t = *reinterpret_cast<const float4*>(gk + k1);
+          u[k1] = make_float2(t.x, t.y);
+          u[k1 + 1] = make_float2(t.z, t.w);
         }
       }
-    } else {
-      // C2: increment dt G J'_hat / den_c  (:976)
-      const float2 jp = U0[a];
-      const float q4 = qx4 + __ldg(sh.qy4 + ky) + __ldg(sh.qz4 + kz);
-      const float dd = rp.D_L * rp.dt;
-      const float den = fmaf(dd * rp.kappa_c, q4, 1.0f);
-      const float g = qnx + qn_y + qn_z;
-      const float s = rp.dt * g * inv_nyz / den;
-      U0[a] = cmul_pi(make_float2(jp.x * s, jp.y * s));
+#pragma unroll
+      for (int k1 = 0; k1 < N1z; ++k1) {
+        const int kz = k2 + N2z * k1;
+        const float2 dd = make_float2(d[k1].x * inv_nyz, d[k1].y * inv_nyz);  // normalised D_hat
+        if (MODE == YZ_IMPORT) {
+          u[k1] = dd;
+          continue;
+        }
+        const float q2 = qx2 + qy2 + __ldg(sh.qz2 + kz);
+        const float qn_z = __ldg(sh.qnz + kz);
+        const float2 uu = u[k1];
+        if (MODE == YZ_MAIN) {
+          const float kn2 = qnx * qnx + qn_y * qn_y + qn_z * qn_z;
+          fint = fmaf(kn2, uu.x * uu.x + uu.y * uu.y, fint);
+          if (!is_c) {
+            // AC (:1015-1024): u += (-L dt kappa q^2 u - L dt D) / (1 + L kappa dt q^2)
+            const float lk = rp.L * rp.dt;
+            const float den = fmaf(lk * rp.kappa_phi, q2, 1.0f);
+            const float inv = 1.0f / den;
+            const float m1 = -lk * rp.kappa_phi * q2 * inv;
+            const float m2 = -lk * inv;
+            u[k1] = make_float2(uu.x + fmaf(m1, uu.x, m2 * dd.x), uu.y + fmaf(m1, uu.y, m2 * dd.y));
+          } else {
+            // CH (:976-983): c += (-D dt kappa_c K4 c + D K2 dt mu) / (1 + D dt kappa_c K4), K2 = -q^2
+            const float q4 = qx4 + qy4 + __ldg(sh.qz4 + kz);
+            const float dm = rp.D_L * rp.dt;
+            const float den = fmaf(dm * rp.kappa_c, q4, 1.0f);
+            const float inv = 1.0f / den;
+            const float m1 = -dm * rp.kappa_c * q4 * inv;
+            const float m2 = -dm * q2 * inv;
+            u[k1] = make_float2(uu.x + fmaf(m1, uu.x, m2 * dd.x), uu.y + fmaf(m1, uu.y, m2 * dd.y));
+            if (var_c) {
+              // J_hat = G mu_hat - kappa_c c_hat K3 (:932-935), G = i g, K3 = i k3;
+              // the d registers carry J_hat to the inverse transform
+              const float g = qnx + qn_y + qn_z;
+              const float k3 = -(qnx * qx2 + qn_y * qy2 + qn_z * __ldg(sh.qz2 + kz));
+              d[k1] = cmul_pi(make_float2(g * dd.x - rp.kappa_c * k3 * uu.x, g * dd.y - rp.kappa_c * k3 * uu.y));
+            }
+          }
+        } else {
+          // C2: c += dt G J'_hat / (1 + D dt kappa_c K4)  (:976)
+          const float q4 = qx4 + qy4 + __ldg(sh.qz4 + kz);
+          const float dm = rp.D_L * rp.dt;
+          const float den = fmaf(dm * rp.kappa_c, q4, 1.0f);
+          const float g = qnx + qn_y + qn_z;
+          const float s = rp.dt * g / den;
+          u[k1] = cadd(uu, cmul_pi(make_float2(dd.x * s, dd.y * s)));
+        }
+      }
+#pragma unroll
+      for (int k1 = 0; k1 < N1z; k1 += 2)
+        *reinterpret_cast<float4*>(gk + k1) = make_float4(u[k1].x, u[k1].y, u[k1 + 1].x, u[k1 + 1].y);
+      if (MODE != YZ_IMPORT) {
+        if (var_c) {
+          dft_inv<N1z>(d);
+#pragma unroll
+          for (int k1 = 0; k1 < N1z; ++k1) pb[k1] = d[k1];
+        } else {
+          dft_inv<N1z>(u);
+#pragma unroll
+          for (int k1 = 0; k1 < N1z; ++k1) pb[k1] = u[k1];
+        }
+      }
     }
+  }
+  if (MODE == YZ_IMPORT) {
+    cluster_barrier<C>();  // peers may still read this CTA's A buffer
+    return;
   }
   __syncthreads();
-  // 6. inverse z transforms
-  fft_inv_lines<NZ>(U0, G::LB, G::PZ, sh.twZ);
-  if (MODE == YZ_MAIN && var_c) fft_inv_lines<NZ>(U1, G::LB, G::PZ, sh.twZ);
+  passA<NZ, G::LB, G::PZ, T, true>(UB, sh.twZ);
   cluster_barrier<C>();
-  // 7. B -> A exchanges: increment -> U2 (, J_hat -> U0)
-  exch_BA<NY, NZ, C>(U2, rU[0], r);
-  if (MODE == YZ_MAIN && var_c) {
-    cluster_barrier<C>();
-    exch_BA<NY, NZ, C>(U0, rU[1], r);
-  }
+  exch_BA<NY, NZ, C, T>(UA, smem_addr(UB), r);
   cluster_barrier<C>();  // no CTA reads a peer's buffers after this point
-  // 8. inverse y transforms
-  fft_inv_lines<NY>(U2, G::LA, G::PY, sh.twY);
-  if (MODE == YZ_MAIN && var_c) fft_inv_lines<NY>(U0, G::LA, G::PY, sh.twY);
+  passB<NY, G::LA, G::PY, T, true>(UA);
+  __syncthreads();
 
-  // 9. epilogue
-  const bool real_plane = (kx == 0) || (2 * kx == sh.Nx);  // x-DFT of real data is real here
-  constexpr int TOT = G::LA * NY / 2;
-  if (MODE == YZ_MAIN && var_c) {
-    float2* Ag = rp.A + kx * plane_elems;
-    float2* Jg = rp.J + kx * plane_elems;
-    for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
-      const int y2 = i % (NY / 2), zl = i / (NY / 2);
-      const int s = zl * G::PY + Line<NY>::phys(2 * y2);
-      const size_t g = (size_t)(z0 + zl) * NY + 2 * y2;
-      const float2 a0 = U2[s], a1 = U2[s + 1];
-      const float2 j0 = U0[s], j1 = U0[s + 1];
-      *reinterpret_cast<float4*>(Ag + g) = make_float4(a0.x, a0.y, a1.x, a1.y);
-      *reinterpret_cast<float4*>(Jg + g) = make_float4(j0.x, j0.y, j1.x, j1.y);
-    }
-  } else {
-    float2* Sg = rp.S + f * fstride + kx * plane_elems;
-    const float2* Ag = (MODE == YZ_C2) ? rp.A + kx * plane_elems : nullptr;
-    constexpr int K = 4;
-    for (int base = threadIdx.x; base < TOT; base += blockDim.x * K) {
-      float4 sv[K], av[K];
+  // 3. last inverse y pass straight to the mixed-space output
+  //    (u~ for the next x pass, or J~ for the variable-mobility chain)
+  {
+    const bool real_plane = (kx == 0) || (2 * kx == sh.Nx);  // the x-DFT of real data is real there
+    float2* dst = var_c ? rp.J + kx * plane_elems : rp.Sm + poff;
+    const int n1 = threadIdx.x % N1y;
+    float2 w[N2y];
 #pragma unroll
-      for (int k = 0; k < K; ++k) {
-        const int i = base + k * blockDim.x;
-        if (i < TOT) {
-          const int y2 = i % (NY / 2), zl = i / (NY / 2);
-          const size_t g = (size_t)(z0 + zl) * NY + 2 * y2;
-          sv[k] = *reinterpret_cast<const float4*>(Sg + g);
-          if (MODE == YZ_C2) av[k] = *reinterpret_cast<const float4*>(Ag + g);
-        }
-      }
+    for (int k2 = 1; k2 < N2y; ++k2) w[k2] = __ldg(sh.twY + n1 * k2);
+    constexpr int ITEMS = G::LA * N1y, ITER = (ITEMS + T - 1) / T;
 #pragma unroll
-      for (int k = 0; k < K; ++k) {
-        const int i = base + k * blockDim.x;
-        if (i < TOT) {
-          const int y2 = i % (NY / 2), zl = i / (NY / 2);
-          const size_t g = (size_t)(z0 + zl) * NY + 2 * y2;
-          const int s = zl * G::PY + Line<NY>::phys(2 * y2);
-          const float2 d0 = U2[s], d1 = U2[s + 1];
-          float4 o = make_float4(sv[k].x + d0.x, sv[k].y + d0.y, sv[k].z + d1.x, sv[k].w + d1.y);
-          if (MODE == YZ_C2) { o.x += av[k].x; o.y += av[k].y; o.z += av[k].z; o.w += av[k].w; }
-          if (real_plane) { o.y = 0.f; o.w = 0.f; }
-          *reinterpret_cast<float4*>(Sg + g) = o;
-        }
+    for (int j = 0; j < ITER; ++j) {
+      const int it = threadIdx.x + j * T;
+      if (ITEMS % T != 0 && it >= ITEMS) break;
+      const int zl = it / N1y;
+      const float2* s = UA + zl * G::PY + n1;
+      float2 v[N2y];
+      v[0] = s[0];
+#pragma unroll
+      for (int k2 = 1; k2 < N2y; ++k2) v[k2] = cmulc(s[k2 * (N1y + 1)], w[k2]);
+      dft_inv<N2y>(v);
+      float2* o = dst + (size_t)(z0 + zl) * NY + n1;
+#pragma unroll
+      for (int n2 = 0; n2 < N2y; ++n2) {
+        float2 x = v[n2];
+        if (real_plane && !var_c) x.y = 0.f;
+        o[n2 * N1y] = x;
       }
     }
   }
@@ -697,11 +783,11 @@ __global__ void __launch_bounds__(512) yz_kernel(const RunParams* __restrict__ r
     __syncthreads();
     if (threadIdx.x == 0) {
       double s = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+#pragma unroll
+      for (int w = 0; w < T / 32; ++w) s += red[w];
       const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
       const double n3 = (double)sh.Nx * NY * NZ;
-      const double nyz = (double)NY * NZ;
-      rp.part_yz[blockIdx.x] = s * wkx * 0.5 * kap * n3 / (nyz * nyz);
+      rp.part_yz[blockIdx.x] = s * wkx * 0.5 * kap * n3;
     }
   }
 }

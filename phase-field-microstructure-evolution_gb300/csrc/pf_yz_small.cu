@@ -5,8 +5,9 @@ namespace pf {
 
 template <int NY, int NZ, int C, int T>
 static void fill(YZKernels* k) {
-  k->main = yz_kernel<NY, NZ, C, YZ_MAIN>;
-  k->c2 = yz_kernel<NY, NZ, C, YZ_C2>;
+  k->main = yz_kernel<NY, NZ, C, T, YZ_MAIN>;
+  k->c2 = yz_kernel<NY, NZ, C, T, YZ_C2>;
+  k->imp = yz_kernel<NY, NZ, C, T, YZ_IMPORT>;
   k->cluster = C;
   k->threads = T;
   k->smem = YZ<NY, NZ, C>::SMEM;

@@ -23,6 +23,7 @@ EXPORTED = (
     "pf_create", "pf_supported_shape", "pf_set_fields", "pf_step", "pf_get_fields", "pf_destroy",
     "pf_last_error", "pf_batch_create", "pf_batch_set_fields", "pf_batch_step", "pf_batch_get_fields",
     "pf_batch_destroy", "f_trans_", "inv_trans_", "k_space_", "pf_shim_device", "pf_ran2_init", "pf_ran2",
+    "pf_ic_noise", "pf_ic_voronoi",
 )
 
 
@@ -104,6 +105,8 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_shim_device": (C.c_int, [C.c_int]),
         "pf_ran2_init": (None, [P(Ran2State)]),
         "pf_ran2": (C.c_double, [P(Ran2State), ip]),
+        "pf_ic_noise": (C.c_int, [P(Config), C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]),
+        "pf_ic_voronoi": (C.c_int, [P(Config), C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -161,6 +164,13 @@ class Run:
         a = to_aos(phi)
         c = np.ascontiguousarray(con, dtype=np.float64)
         _check(self.lib.pf_set_fields(self.h, _dp(a), _dp(c)))
+
+    def set_fields_aos(self, phi_aos: np.ndarray, con: np.ndarray):
+        """Upload buffers already in the Fortran phi(var,x,y,z) layout."""
+        _check(self.lib.pf_set_fields(self.h, _dp(phi_aos), _dp(con)))
+
+    def get_fields_aos(self, phi_aos: np.ndarray, con: np.ndarray):
+        _check(self.lib.pf_get_fields(self.h, _dp(phi_aos), _dp(con)))
 
     def step(self, n: int, raise_nonfinite: bool = True) -> List[dict]:
         d = (Diag * max(n, 1))()
@@ -231,6 +241,45 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def _ic_buffers(p, pinned: bool):
+    shape_phi = (p.Nz, p.Ny, p.Nx, p.var)
+    shape_c = (p.Nz, p.Ny, p.Nx)
+    if pinned:
+        import torch
+
+        a = torch.empty(shape_phi, dtype=torch.float64, pin_memory=True).numpy()
+        c = torch.empty(shape_c, dtype=torch.float64, pin_memory=True).numpy()
+        return a, c
+    return np.empty(shape_phi), np.empty(shape_c)
+
+
+def ic_noise_aos(p, seed: int, amp_phi: float, c0: float, amp_c: float, pinned: bool = False):
+    """Noise start in the Fortran layout of the C ABI: (phi(var,x,y,z), con)."""
+    lib = load_library()
+    a, c = _ic_buffers(p, pinned)
+    cfg = make_config(p)
+    _check(lib.pf_ic_noise(C.byref(cfg), seed, amp_phi, c0, amp_c, _dp(a), _dp(c)))
+    return a, c
+
+
+def ic_voronoi_aos(p, seed: int, n_grains: int, amp_phi: float, c0: float, amp_c: float, pinned: bool = False):
+    lib = load_library()
+    a, c = _ic_buffers(p, pinned)
+    cfg = make_config(p)
+    _check(lib.pf_ic_voronoi(C.byref(cfg), seed, n_grains, amp_phi, c0, amp_c, _dp(a), _dp(c)))
+    return a, c
+
+
+def ic_noise(p, seed, amp_phi, c0, amp_c):
+    a, c = ic_noise_aos(p, seed, amp_phi, c0, amp_c)
+    return from_aos(a), c
+
+
+def ic_voronoi(p, seed, n_grains, amp_phi, c0, amp_c):
+    a, c = ic_voronoi_aos(p, seed, n_grains, amp_phi, c0, amp_c)
+    return from_aos(a), c
 
 
 class Ran2:

@@ -58,3 +58,15 @@ def test_k_space_shim_matches_oracle(lib, oracle):
     assert np.allclose(kfc.sum(-1), G, atol=1e-15)
     assert np.allclose(ksq[..., 0].reshape(Nx // 2 + 1, Ny, Nz, 3).transpose(2, 1, 0, 3).sum(-1), K2)
     assert np.allclose(k4[..., 0].reshape(Nx // 2 + 1, Ny, Nz, 3).transpose(2, 1, 0, 3).sum(-1), K4)
+
+
+@pytest.mark.parametrize("kind", ["noise", "voronoi"])
+def test_library_ics_match_oracle(pkg, oracle, kind):
+    p = oracle.Params(12, 10, 8, 3)
+    if kind == "noise":
+        a = pkg.ic_noise(p, 3, 0.01, 0.45, 0.02)
+        b = oracle.ic_noise(p, 3, 0.01, 0.45, 0.02)
+    else:
+        a = pkg.ic_voronoi(p, 4, 7, 0.01, 0.5, 0.02)
+        b = oracle.ic_voronoi(p, 4, 7, 0.01, 0.5, 0.02)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
