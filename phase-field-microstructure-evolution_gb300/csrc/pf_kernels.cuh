@@ -97,57 +97,176 @@ __device__ __forceinline__ float warp_max(float v) {
 }
 
 // ---------------------------------------------------------------------------
-// x-direction half-spectrum <-> interleaved real line (length M = Nx/2 complex)
+// x-direction half spectrum <-> interleaved real line (M = Nx/2 complex).
+// With z[m] = x[2m] + i x[2m+1] and Z = DFT_M(z):
+//   X[k] = (Z[k] + conj Z[M-k])/2 - (i/2) W_N^k (Z[k] - conj Z[M-k]),
+//   X[0] = Re Z0 + Im Z0,  X[M] = Re Z0 - Im Z0;
+// the inverse builds Z'[k] = (X[k] + conj X[M-k]) + i conj(W_N^k) (X[k] - conj X[M-k])
+// so that IDFT_M(Z') = N z.  Frequencies k and M-k always sit in mirrored
+// runs of the four-step layout, so one thread owns both halves of every pair.
 // ---------------------------------------------------------------------------
-// C2R pre-processing of the pair (k, M-k) into digit-transposed positions.
-// X = normalised half spectrum; output Z' such that IDFT_M(Z')[m] = x[2m] + i x[2m+1].
-template <int M>
-__device__ __forceinline__ void c2r_pre(float2* line, int k, float2 Xk, float2 Xmk, const float2* __restrict__ twN) {
-  using LM = Line<M>;
-  if (k == 0) {
-    line[LM::phys(LM::pos_of_freq(0))] = make_float2(Xk.x + Xmk.x, Xk.x - Xmk.x);
-    return;
-  }
-  {
-    const float2 w = __ldg(twN + k);
-    const float2 b = cconj(Xmk);
-    const float2 s = cadd(Xk, b), d = csub(Xk, b);
-    line[LM::phys(LM::pos_of_freq(k))] = cadd(s, cmul_pi(cmulc(d, w)));
-  }
-  if (2 * k != M) {
-    const float2 w = __ldg(twN + (M - k));
-    const float2 b = cconj(Xk);
-    const float2 s = cadd(Xmk, b), d = csub(Xmk, b);
-    line[LM::phys(LM::pos_of_freq(M - k))] = cadd(s, cmul_pi(cmulc(d, w)));
+// inverse pre-processing of the pair (k, M-k), 0 < k < M
+__device__ __forceinline__ void pre_pair(float2 xk, float2 xm, float2 wk, float2 wm, float2& zk, float2& zm) {
+  const float2 s = cadd(xk, cconj(xm)), d = csub(xk, cconj(xm));
+  zk = cadd(s, cmul_pi(cmulc(d, wk)));
+  // s' = conj(s), d' = -conj(d)
+  const float2 d2 = make_float2(-d.x, d.y);
+  zm = cadd(cconj(s), cmul_pi(cmulc(d2, wm)));
+}
+// forward post-processing of the pair (k, M-k), 0 < k < M, scaled by h = scale/2
+__device__ __forceinline__ void post_pair(float2 zk, float2 zm, float2 wk, float2 wm, float h, float2& xk, float2& xm) {
+  const float2 s = cadd(zk, cconj(zm)), d = csub(zk, cconj(zm));
+  xk = cscale(cadd(s, cmul_mi(cmul(d, wk))), h);
+  const float2 d2 = make_float2(-d.x, d.y);
+  xm = cscale(cadd(cconj(s), cmul_mi(cmul(d2, wm))), h);
+}
+
+// pass A over a runtime number of lines (pitch P, T threads)
+template <int L, int P, int T, bool INV>
+__device__ __forceinline__ void passA_rt(float2* buf, int NL, const float2* __restrict__ tw) {
+  constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
+  static_assert(T % N1 == 0, "threads must be a multiple of N1");
+  const int n1 = threadIdx.x % N1;
+  float2 w[N2];
+#pragma unroll
+  for (int k2 = 1; k2 < N2; ++k2) w[k2] = __ldg(tw + n1 * k2);
+  for (int l = threadIdx.x / N1; l < NL; l += T / N1) {
+    float2* p = buf + l * P + n1;
+    float2 v[N2];
+    if (!INV) {
+#pragma unroll
+      for (int n2 = 0; n2 < N2; ++n2) v[n2] = p[n2 * (N1 + 1)];
+      Dft<N2>::fwd(v);
+#pragma unroll
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], w[k2]);
+    } else {
+      v[0] = p[0];
+#pragma unroll
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * (N1 + 1)], w[k2]);
+      dft_inv<N2>(v);
+    }
+#pragma unroll
+    for (int k = 0; k < N2; ++k) p[k * (N1 + 1)] = v[k];
   }
 }
 
-// R2C post-processing: from Z = DFT_M(x[2m] + i x[2m+1]) (digit-transposed) to
-// X[k], X[M-k] scaled by `scale` (X[0] and X[M] are real).
+// Inverse x transform, first half: read the half spectrum of line (f, yy)
+// from global for the run pair `pr`, pre-process, inverse DFT_N1 of each run,
+// store the runs (pass B' output) into the padded line.
 template <int M>
-__device__ __forceinline__ void r2c_post(const float2* line, int k, float scale, const float2* __restrict__ twN,
-                                         float2& Xk, float2& Xmk) {
-  using LM = Line<M>;
-  if (k == 0) {
-    const float2 z0 = line[LM::phys(LM::pos_of_freq(0))];
-    Xk = make_float2((z0.x + z0.y) * scale, 0.f);
-    Xmk = make_float2((z0.x - z0.y) * scale, 0.f);
-    return;
+__device__ __forceinline__ void x_inv_runs(const float2* __restrict__ src, size_t plane, float2* line, int pr,
+                                           const float2* __restrict__ twN) {
+  constexpr int N1 = Line<M>::N1, N2 = Line<M>::N2;
+  if (pr > 0 && 2 * pr < N2) {
+    const int ra = pr, rb = N2 - pr;
+    float2 a[N1], b[N1];
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) {
+      a[k1] = __ldg(src + (size_t)(ra + N2 * k1) * plane);
+      b[k1] = __ldg(src + (size_t)(rb + N2 * k1) * plane);
+    }
+    float2 za[N1], zb[N1];
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) {
+      const int k = ra + N2 * k1;
+      pre_pair(a[k1], b[N1 - 1 - k1], __ldg(twN + k), __ldg(twN + M - k), za[k1], zb[N1 - 1 - k1]);
+    }
+    dft_inv<N1>(za);
+    dft_inv<N1>(zb);
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) {
+      line[n1 + (N1 + 1) * ra] = za[n1];
+      line[n1 + (N1 + 1) * rb] = zb[n1];
+    }
+  } else if (pr == 0) {
+    float2 a[N1];
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = __ldg(src + (size_t)(N2 * k1) * plane);
+    const float2 xM = __ldg(src + (size_t)M * plane);
+    float2 z[N1];
+    z[0] = make_float2(a[0].x + xM.x, a[0].x - xM.x);
+#pragma unroll
+    for (int k1 = 1; k1 <= N1 / 2; ++k1) {
+      const int k = N2 * k1;
+      float2 zk, zm;
+      pre_pair(a[k1], a[N1 - k1], __ldg(twN + k), __ldg(twN + M - k), zk, zm);
+      z[k1] = zk;
+      if (k1 != N1 - k1) z[N1 - k1] = zm;
+    }
+    dft_inv<N1>(z);
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) line[n1] = z[n1];
+  } else {  // pr == N2/2: the run pairs with itself, element k1 with N1-1-k1
+    const int ra = N2 / 2;
+    float2 a[N1];
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = __ldg(src + (size_t)(ra + N2 * k1) * plane);
+    float2 z[N1];
+#pragma unroll
+    for (int k1 = 0; k1 < N1 / 2; ++k1) {
+      const int k = ra + N2 * k1;
+      pre_pair(a[k1], a[N1 - 1 - k1], __ldg(twN + k), __ldg(twN + M - k), z[k1], z[N1 - 1 - k1]);
+    }
+    dft_inv<N1>(z);
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) line[n1 + (N1 + 1) * ra] = z[n1];
   }
-  const float2 zk = line[LM::phys(LM::pos_of_freq(k))];
-  const float2 zm = line[LM::phys(LM::pos_of_freq(M - k))];
+}
+
+// Forward x transform, last half: forward DFT_N1 of the run pair `pr` (pass
+// B), post-process, store the half spectrum (scaled) to global.
+template <int M>
+__device__ __forceinline__ void x_fwd_runs(float2* __restrict__ dst, size_t plane, const float2* line, int pr,
+                                           float scale, const float2* __restrict__ twN) {
+  constexpr int N1 = Line<M>::N1, N2 = Line<M>::N2;
   const float h = 0.5f * scale;
-  {
-    const float2 b = cconj(zm);
-    const float2 s = cadd(zk, b), d = csub(zk, b);
-    const float2 t = cmul_mi(cmul(d, __ldg(twN + k)));
-    Xk = cscale(cadd(s, t), h);
-  }
-  {
-    const float2 b = cconj(zk);
-    const float2 s = cadd(zm, b), d = csub(zm, b);
-    const float2 t = cmul_mi(cmul(d, __ldg(twN + (M - k))));
-    Xmk = cscale(cadd(s, t), h);
+  if (pr > 0 && 2 * pr < N2) {
+    const int ra = pr, rb = N2 - pr;
+    float2 za[N1], zb[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) {
+      za[n1] = line[n1 + (N1 + 1) * ra];
+      zb[n1] = line[n1 + (N1 + 1) * rb];
+    }
+    Dft<N1>::fwd(za);
+    Dft<N1>::fwd(zb);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) {
+      const int k = ra + N2 * k1;
+      float2 xk, xm;
+      post_pair(za[k1], zb[N1 - 1 - k1], __ldg(twN + k), __ldg(twN + M - k), h, xk, xm);
+      dst[(size_t)k * plane] = xk;
+      dst[(size_t)(M - k) * plane] = xm;
+    }
+  } else if (pr == 0) {
+    float2 z[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) z[n1] = line[n1];
+    Dft<N1>::fwd(z);
+    dst[0] = make_float2((z[0].x + z[0].y) * scale, 0.f);
+    dst[(size_t)M * plane] = make_float2((z[0].x - z[0].y) * scale, 0.f);
+#pragma unroll
+    for (int k1 = 1; k1 <= N1 / 2; ++k1) {
+      const int k = N2 * k1;
+      float2 xk, xm;
+      post_pair(z[k1], z[N1 - k1], __ldg(twN + k), __ldg(twN + M - k), h, xk, xm);
+      dst[(size_t)k * plane] = xk;
+      if (k1 != N1 - k1) dst[(size_t)(M - k) * plane] = xm;
+    }
+  } else {
+    const int ra = N2 / 2;
+    float2 z[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) z[n1] = line[n1 + (N1 + 1) * ra];
+    Dft<N1>::fwd(z);
+#pragma unroll
+    for (int k1 = 0; k1 < N1 / 2; ++k1) {
+      const int k = ra + N2 * k1;
+      float2 xk, xm;
+      post_pair(z[k1], z[N1 - 1 - k1], __ldg(twN + k), __ldg(twN + M - k), h, xk, xm);
+      dst[(size_t)k * plane] = xk;
+      dst[(size_t)(M - k) * plane] = xm;
+    }
   }
 }
 
@@ -271,12 +390,13 @@ __device__ __forceinline__ void bulk_cell(float2* smem, int yy, int slot, int se
 // ---------------------------------------------------------------------------
 enum XMode { MODE_BULK = 0, MODE_XJ = 1, MODE_IMPORT = 2, MODE_EXPORT = 3 };
 
-template <int NX, int WY, int MODE>
-__global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict__ runs, const Shape sh) {
+template <int NX, int WY, int T, int MODE>
+__global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   constexpr int M = NX / 2;
   using LM = Line<M>;
   constexpr int PM = LM::PITCH;
-  constexpr int NPAIR = M / 2 + 1;
+  constexpr int NP = LM::N2 / 2 + 1;  // run pairs per line
+  static_assert(LM::N2 % 2 == 0, "x plan needs an even number of runs");
   extern __shared__ float2 smem[];
   const RunParams& rp = runs[blockIdx.y];
   const int nF = (MODE == MODE_XJ) ? 1 : rp.V + 1;
@@ -290,28 +410,24 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
 
   if (MODE == MODE_IMPORT) {
     // real rows -> interleaved lines (natural order)
-    for (int it = threadIdx.x; it < nF * WY * M; it += blockDim.x) {
+    for (int it = threadIdx.x; it < nF * WY * M; it += T) {
       const int m = it % M, r = it / M, yy = r % WY, f = r / WY;
       const float2 v = *reinterpret_cast<const float2*>(rp.fin + (((size_t)f * sh.Nz + z) * sh.Ny + y0 + yy) * NX + 2 * m);
       smem[(f * WY + yy) * PM + LM::phys(m)] = v;
     }
-    __syncthreads();
   } else {
-    // 1. load the half-spectrum rows, C2R pre-processing
-    for (int it = threadIdx.x; it < nF * WY * NPAIR; it += blockDim.x) {
-      const int yy = it % WY, r = it / WY, k = r % NPAIR, f = r / NPAIR;
-      const float2* sf = src + f * fstride + row_off + yy;
-      const float2 xk = sf[(size_t)k * plane];
-      const float2 xm = sf[(size_t)(M - k) * plane];
-      c2r_pre<M>(smem + (f * WY + yy) * PM, k, xk, xm, sh.twN);
+    // 1. inverse x transform: global half spectrum -> pre-processing -> pass B'
+    for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
+      const int yy = it % WY, r = it / WY, pr = r % NP, f = r / NP;
+      x_inv_runs<M>(src + f * fstride + row_off + yy, plane, smem + (f * WY + yy) * PM, pr, sh.twN);
     }
     __syncthreads();
-    // 2. inverse x transform -> interleaved real values (natural order)
-    fft_inv_lines<M>(smem, nF * WY, PM, sh.twM);
+    passA_rt<M, PM, T, true>(smem, nF * WY, sh.twM);
   }
+  __syncthreads();
 
   if (MODE == MODE_EXPORT) {
-    for (int it = threadIdx.x; it < nF * WY * M; it += blockDim.x) {
+    for (int it = threadIdx.x; it < nF * WY * M; it += T) {
       const int m = it % M, r = it / M, yy = r % WY, f = r / WY;
       *reinterpret_cast<float2*>(rp.fin + (((size_t)f * sh.Nz + z) * sh.Ny + y0 + yy) * NX + 2 * m) =
           smem[(f * WY + yy) * PM + LM::phys(m)];
@@ -325,8 +441,8 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
   acc.nonfinite = 0;
 
   if (MODE == MODE_BULK) {
-    // 3. bulk terms, two cells per slot
-    for (int it = threadIdx.x; it < WY * M; it += blockDim.x) {
+    // 2. bulk terms, two cells per slot
+    for (int it = threadIdx.x; it < WY * M; it += T) {
       const int m = it % M, yy = it / M;
       const int slot = LM::phys(m);
       float dfdc0, dfdc1, mob0, mob1;
@@ -338,7 +454,7 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
     }
     __syncthreads();
   } else if (MODE == MODE_XJ) {
-    for (int it = threadIdx.x; it < WY * M; it += blockDim.x) {
+    for (int it = threadIdx.x; it < WY * M; it += T) {
       const int m = it % M, yy = it / M;
       const int slot = LM::phys(m);
       const float2 mb = *reinterpret_cast<const float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m);
@@ -350,17 +466,14 @@ __global__ void __launch_bounds__(256) x_pass_kernel(const RunParams* __restrict
     __syncthreads();
   }
 
-  // 4. forward x transform and 5. R2C post-processing, scaled by 1/Nx
-  fft_fwd_lines<M>(smem, nF * WY, PM, sh.twM);
+  // 3. forward x transform: pass A, then pass B + post-processing -> global
+  passA_rt<M, PM, T, false>(smem, nF * WY, sh.twM);
+  __syncthreads();
   float2* __restrict__ dst = (MODE == MODE_BULK) ? rp.D : (MODE == MODE_XJ ? rp.J : rp.Sm);
   const float scale = 1.0f / (float)NX;
-  for (int it = threadIdx.x; it < nF * WY * NPAIR; it += blockDim.x) {
-    const int yy = it % WY, r = it / WY, k = r % NPAIR, f = r / NPAIR;
-    float2 xk, xm;
-    r2c_post<M>(smem + (f * WY + yy) * PM, k, scale, sh.twN, xk, xm);
-    float2* df = dst + f * fstride + row_off + yy;
-    df[(size_t)k * plane] = xk;
-    if (2 * k != M) df[(size_t)(M - k) * plane] = xm;
+  for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
+    const int yy = it % WY, r = it / WY, pr = r % NP, f = r / NP;
+    x_fwd_runs<M>(dst + f * fstride + row_off + yy, plane, smem + (f * WY + yy) * PM, pr, scale, sh.twN);
   }
 
   if (MODE != MODE_BULK) return;

@@ -7,10 +7,10 @@ namespace pf {
 
 template <int NX, int WY>
 static void fill(XKernels* k) {
-  k->bulk = x_pass_kernel<NX, WY, MODE_BULK>;
-  k->xj = x_pass_kernel<NX, WY, MODE_XJ>;
-  k->imp = x_pass_kernel<NX, WY, MODE_IMPORT>;
-  k->exp = x_pass_kernel<NX, WY, MODE_EXPORT>;
+  k->bulk = x_pass_kernel<NX, WY, 256, MODE_BULK>;
+  k->xj = x_pass_kernel<NX, WY, 256, MODE_XJ>;
+  k->imp = x_pass_kernel<NX, WY, 256, MODE_IMPORT>;
+  k->exp = x_pass_kernel<NX, WY, 256, MODE_EXPORT>;
   k->wy = WY;
 }
 
