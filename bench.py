@@ -63,8 +63,11 @@ class Clocks:
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.skip = 0
 
     def start(self):
+        """Start sampling and wait for the first samples, so that nvidia-smi's
+        own start-up does not overlap the timed region."""
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
@@ -73,7 +76,21 @@ class Clocks:
                  "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
-        time.sleep(0.3)
+            return
+        t0 = time.time()
+        while time.time() - t0 < 20.0:
+            with open(self.path) as fh:
+                if len(fh.readlines()) >= 3:
+                    break
+            time.sleep(0.05)
+        with open(self.path) as fh:
+            self.skip = len(fh.readlines())
+
+    def mark(self):
+        """Count only the samples taken from now on."""
+        if self.proc is not None:
+            with open(self.path) as fh:
+                self.skip = len(fh.readlines())
 
     def stop(self):
         if self.proc is None:
@@ -82,7 +99,7 @@ class Clocks:
         self.proc.wait()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for line in open(self.path).readlines()[self.skip:]:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -216,16 +233,17 @@ def run_ours(args):
         if dist is not None:
             dist.barrier()
 
+    clocks = Clocks(local)
+    clocks.start()
     # warm-up
     lib.pf_batch_enqueue(b, args.warmup)
     torch.cuda.synchronize()
 
     # timed region: K steps on the library's stream
-    clocks = Clocks(local)
-    clocks.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     barrier()
+    clocks.mark()
     ev0.record(ext)
     rc = lib.pf_batch_enqueue(b, args.steps)
     ev1.record(ext)

@@ -271,9 +271,8 @@ __device__ __forceinline__ void x_fwd_runs(float2* __restrict__ dst, size_t plan
 }
 
 // ---------------------------------------------------------------------------
-// Bulk terms of one cell (src/var_diff.f90:685-898), reading/writing the
-// interleaved real lines of all fields.  `sel` picks the x (0) or y (1)
-// component of the float2 slot, i.e. cell x = 2m + sel.
+// Bulk terms (src/var_diff.f90:685-898) on the interleaved real lines of all
+// fields.
 // ---------------------------------------------------------------------------
 struct BulkAcc {
   float feta, fch, mass;  // per-thread partial sums over a few cells (FP64 from the warp level up)
@@ -281,106 +280,121 @@ struct BulkAcc {
   int nonfinite;
 };
 
-__device__ __forceinline__ float get_c(const float2& v, int sel) { return sel ? v.y : v.x; }
-__device__ __forceinline__ void set_c(float2& v, int sel, float a) {
-  if (sel) v.y = a; else v.x = a;
-}
-
+// Bulk terms of the two cells x = 2m, 2m+1 held in one float2 slot of every
+// field line.  Pass 1 forms the per-cell aggregates, pass 2 overwrites each
+// phi slot with dF/dphi_i; dF/dc and the mobility are returned.
 template <int PM, int WY>
-__device__ __forceinline__ void bulk_cell(float2* smem, int yy, int slot, int sel, const RunParams& rp,
-                                          float& dfdc_out, float& mob_out, BulkAcc& acc) {
+__device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const RunParams& rp, float2& dfdc,
+                                          float2& mob, BulkAcc& acc) {
   const int V = rp.V;
   const float sg1 = rp.sigma1, sg2 = rp.sigma2;
-  // pass 1: aggregates.  S2 = sum phi^2, Smat = sum_{i<V-1} phi^2,
-  // S4 = sum phi^4, N4 = sum_{i<V-1} phi^4, prefix pair sum for f_eta.
-  float S2 = 0.f, Smat = 0.f, S4 = 0.f, N4 = 0.f, pairs = 0.f, pre = 0.f, mabs = 0.f;
+  float2* base = smem + yy * PM + slot;
+  constexpr int FS = WY * PM;  // stride between fields
+  // pass 1: S2 = sum phi^2, Smat = sum_{i<V-1} phi^2, S4, N4, f_eta pair sum
+  float pre0 = 0.f, pre1 = 0.f, n40 = 0.f, n41 = 0.f, pr0 = 0.f, pr1 = 0.f, ma0 = 0.f, ma1 = 0.f;
   for (int f = 0; f < V - 1; ++f) {
-    const float p = get_c(smem[(f * WY + yy) * PM + slot], sel);
-    const float p2 = p * p;
-    pairs = fmaf(p2, pre, pairs);
-    pre += p2;
-    N4 = fmaf(p2, p2, N4);
-    mabs = fmaxf(mabs, fabsf(p));
+    const float2 p = base[f * FS];
+    const float a0 = p.x * p.x, a1 = p.y * p.y;
+    pr0 = fmaf(a0, pre0, pr0);
+    pr1 = fmaf(a1, pre1, pr1);
+    pre0 += a0;
+    pre1 += a1;
+    n40 = fmaf(a0, a0, n40);
+    n41 = fmaf(a1, a1, n41);
+    ma0 = fmaxf(ma0, fabsf(p.x));
+    ma1 = fmaxf(ma1, fabsf(p.y));
   }
-  const float pP = get_c(smem[((V - 1) * WY + yy) * PM + slot], sel);
-  const float pP2 = pP * pP;
-  Smat = pre;
-  S2 = pre + pP2;
-  S4 = N4 + pP2 * pP2;
-  mabs = fmaxf(mabs, fabsf(pP));
-  const float c = get_c(smem[(V * WY + yy) * PM + slot], sel);
-
-  // h = N4/S4 and the term4 ratios.  S4 below 1e-30 (|phi| < ~1e-8) would lose
-  // precision or underflow in FP32: recompute with phi scaled by 1/max|phi|.
-  // All-zero cells give 0/0 in the reference; here they get h = 0, term4 = 0.
-  float invS4, n4n, scale_t4;  // term4 factors use (phi^3/S4)*(phiP^4/S4)
-  bool scaled = false;
-  float inv_m = 1.f;
-  if (S4 >= 1e-30f) {
-    invS4 = 1.f / S4;
-    n4n = N4 * invS4;
-    scale_t4 = 4.f;
-  } else if (mabs > 0.f) {
-    scaled = true;
-    inv_m = 1.f / mabs;
-    float s4 = 0.f, n4 = 0.f;
-    for (int f = 0; f < V - 1; ++f) {
-      const float p = get_c(smem[(f * WY + yy) * PM + slot], sel) * inv_m;
-      const float p2 = p * p;
-      n4 = fmaf(p2, p2, n4);
+  const float2 pP = base[(V - 1) * FS];
+  const float2 cc = base[V * FS];
+  float2 out_df[2];
+  float t4a[2], t4p[2], invm[2], rP4[2];
+  float Smat[2], gP[2];
+  // per-cell scalar work (two cells)
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const float pp = q ? pP.y : pP.x;
+    const float c = q ? cc.y : cc.x;
+    const float pre = q ? pre1 : pre0;
+    const float n4 = q ? n41 : n40;
+    const float pairs = q ? pr1 : pr0;
+    const float mabs = fmaxf(q ? ma1 : ma0, fabsf(pp));
+    const float pp2 = pp * pp;
+    const float S2 = pre + pp2;
+    const float S4 = n4 + pp2 * pp2;
+    // h = N4/S4 and the term4 ratios (phi^3/S4)(phiP^4/S4).  Below S4 = 1e-30
+    // (|phi| < ~1e-8) FP32 would lose them: rescale phi by 1/max|phi|.  All-zero
+    // cells give 0/0 in the reference; here h = 0 and term4 = 0.
+    float invS4, n4n, sc, im = 1.f;
+    if (S4 >= 1e-30f) {
+      invS4 = 1.f / S4;
+      n4n = n4 * invS4;
+      sc = 4.f;
+    } else if (mabs > 0.f) {
+      im = 1.f / mabs;
+      float s4 = 0.f, nn = 0.f;
+      for (int f = 0; f < V - 1; ++f) {
+        const float2 p = base[f * FS];
+        const float x = (q ? p.y : p.x) * im;
+        nn = fmaf(x * x, x * x, nn);
+      }
+      const float xq = pp * im;
+      s4 = nn + (xq * xq) * (xq * xq);
+      invS4 = 1.f / s4;
+      n4n = nn * invS4;
+      sc = 4.f * im;
+    } else {
+      invS4 = 0.f;
+      n4n = 0.f;
+      sc = 0.f;
     }
-    const float q = pP * inv_m;
-    s4 = n4 + (q * q) * (q * q);
-    invS4 = 1.f / s4;
-    n4n = n4 * invS4;
-    scale_t4 = 4.f * inv_m;
-  } else {
-    invS4 = 0.f;
-    n4n = 0.f;
-    scale_t4 = 0.f;
+    const float h = n4n;  // phi_mat (:741)
+    const float dcm = c - rp.c0m, dcp = c - rp.c0p;
+    const float fm = rp.am * dcm * dcm, fp = rp.ap * dcp * dcp;
+    const float dfm = fm - fp;
+    acc.fch += h * fm + (1.f - h) * fp;
+    const float dc = 2.f * h * rp.am * dcm + 2.f * (1.f - h) * rp.ap * dcp;
+    acc.feta += -0.5f * S2 + 0.25f * S4 + sg1 * pairs + sg2 * pp2 * pre;
+    acc.mass += c;
+    acc.cmin = fminf(acc.cmin, c);
+    acc.cmax = fmaxf(acc.cmax, c);
+    acc.phimin = fminf(acc.phimin, S2);
+    acc.phipmax = fmaxf(acc.phipmax, pp);
+    float mb;
+    if (rp.mobility == MOB_REF_VAR) mb = 2.f * (1.f - S2) * rp.D_gb;
+    else if (rp.mobility == MOB_C1MC) mb = rp.D_L * c * (1.f - c);
+    else mb = 0.f;
+    const float qP = pp * im;
+    const float qP2 = qP * qP;
+    rP4[q] = qP2 * qP2 * invS4;           // phiP^4 / S4
+    t4a[q] = sc * invS4 * rP4[q] * dfm;   // term4_i = t4a * q_i^3         (i < V-1)
+    t4p[q] = -sc * (qP * qP2 * invS4) * n4n * dfm;  // term4_P                 (:829-835)
+    invm[q] = im;
+    Smat[q] = pre;
+    gP[q] = sg2 * pp2;
+    out_df[q] = make_float2(dc, mb);
   }
-  const float h = n4n;  // phi_mat (:741)
-  const float dcm = c - rp.c0m, dcp = c - rp.c0p;
-  const float fm = rp.am * dcm * dcm, fp = rp.ap * dcp * dcp;
-  const float dfm = fm - fp;
-  acc.fch += h * fm + (1.f - h) * fp;
-  dfdc_out = 2.f * h * rp.am * dcm + 2.f * (1.f - h) * rp.ap * dcp;
-  acc.feta += -0.5f * S2 + 0.25f * S4 + sg1 * pairs + sg2 * pP2 * Smat;
-  acc.mass += c;
-  acc.cmin = fminf(acc.cmin, c);
-  acc.cmax = fmaxf(acc.cmax, c);
-  acc.phimin = fminf(acc.phimin, S2);
-  acc.phipmax = fmaxf(acc.phipmax, pP);
-  if (rp.mobility == MOB_REF_VAR) mob_out = 2.f * (1.f - S2) * rp.D_gb;
-  else if (rp.mobility == MOB_C1MC) mob_out = rp.D_L * c * (1.f - c);
-  else mob_out = 0.f;
-
+  dfdc = make_float2(out_df[0].x, out_df[1].x);
+  mob = make_float2(out_df[0].y, out_df[1].y);
   // pass 2: dF/dphi_i = phi^3 - phi + 2 phi Gamma_i + term4_i   (:782-857)
-  const float qP = scaled ? pP * inv_m : pP;
-  const float qP2 = qP * qP;
-  const float rP4 = qP2 * qP2 * invS4;  // phiP^4 / S4 (scaled consistently)
-  const float gP = sg2 * pP2;
-  int bad = 0;
+  float dsum = dfdc.x + dfdc.y;
   for (int f = 0; f < V - 1; ++f) {
-    float2& slotv = smem[(f * WY + yy) * PM + slot];
-    const float p = get_c(slotv, sel);
-    const float gam = fmaf(sg1, Smat - p * p, gP);
-    const float q = scaled ? p * inv_m : p;
-    const float t4 = scale_t4 * (q * q * q * invS4) * rP4 * dfm;
-    const float d = fmaf(p, p * p, -p) + 2.f * p * gam + t4;
-    bad |= !isfinite(d);
-    set_c(slotv, sel, d);
+    float2 p = base[f * FS];
+    const float g0 = fmaf(sg1, Smat[0] - p.x * p.x, gP[0]);
+    const float g1 = fmaf(sg1, Smat[1] - p.y * p.y, gP[1]);
+    const float q0 = p.x * invm[0], q1 = p.y * invm[1];
+    const float d0 = fmaf(p.x, p.x * p.x, -p.x) + 2.f * p.x * g0 + t4a[0] * (q0 * q0 * q0);
+    const float d1 = fmaf(p.y, p.y * p.y, -p.y) + 2.f * p.y * g1 + t4a[1] * (q1 * q1 * q1);
+    dsum += d0 + d1;
+    base[f * FS] = make_float2(d0, d1);
   }
   {
-    float2& slotv = smem[((V - 1) * WY + yy) * PM + slot];
-    const float gam = sg2 * Smat;
-    const float t4 = -scale_t4 * (qP * qP2 * invS4) * n4n * dfm;
-    const float d = fmaf(pP, pP2, -pP) + 2.f * pP * gam + t4;
-    bad |= !isfinite(d);
-    set_c(slotv, sel, d);
+    const float g0 = sg2 * Smat[0], g1 = sg2 * Smat[1];
+    const float d0 = fmaf(pP.x, pP.x * pP.x, -pP.x) + 2.f * pP.x * g0 + t4p[0];
+    const float d1 = fmaf(pP.y, pP.y * pP.y, -pP.y) + 2.f * pP.y * g1 + t4p[1];
+    dsum += d0 + d1;
+    base[(V - 1) * FS] = make_float2(d0, d1);
   }
-  bad |= !isfinite(dfdc_out);
-  acc.nonfinite += bad;
+  acc.nonfinite += !isfinite(dsum);  // any NaN/Inf term makes the sum non-finite
 }
 
 // ---------------------------------------------------------------------------
@@ -445,12 +459,11 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
     for (int it = threadIdx.x; it < WY * M; it += T) {
       const int m = it % M, yy = it / M;
       const int slot = LM::phys(m);
-      float dfdc0, dfdc1, mob0, mob1;
-      bulk_cell<PM, WY>(smem, yy, slot, 0, rp, dfdc0, mob0, acc);
-      bulk_cell<PM, WY>(smem, yy, slot, 1, rp, dfdc1, mob1, acc);
-      smem[(rp.V * WY + yy) * PM + slot] = make_float2(dfdc0, dfdc1);
+      float2 dfdc, mob;
+      bulk_slot<PM, WY>(smem, yy, slot, rp, dfdc, mob, acc);
+      smem[(rp.V * WY + yy) * PM + slot] = dfdc;
       if (rp.mobility != MOB_CONST)
-        *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = make_float2(mob0, mob1);
+        *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = mob;
     }
     __syncthreads();
   } else if (MODE == MODE_XJ) {
