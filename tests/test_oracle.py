@@ -155,3 +155,19 @@ def test_circle_ic_shape(oracle):
     assert np.all(phi.sum(axis=0) == 1.0)
     assert phi[1, 12, 12, 12] in (0.0, 1.0)
     assert (phi[2] == 1).sum() > 0 and np.all(con[phi[2] == 1] == 0.7)
+
+
+@pytest.mark.parametrize("name", ["noise_const_16", "voronoi_refvar_16", "voronoi_c1mc_16"])
+def test_oracle_regression_fixtures(oracle, name):
+    import importlib.util
+    from pathlib import Path
+
+    here = Path(__file__).resolve().parent / "golden"
+    spec = importlib.util.spec_from_file_location("make_golden", here / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    ref = np.load(here / f"{name}.npz")
+    ph, c, diag = mg.compute(mg.CASES[name])
+    assert np.allclose(ph, ref["phi"], rtol=0, atol=1e-12)
+    assert np.allclose(c, ref["con"], rtol=0, atol=1e-12)
+    assert np.allclose(diag, ref["diag"], rtol=1e-10, atol=1e-14)
