@@ -335,6 +335,7 @@ def run_ours(args):
                     "what": f"pf_set_fields (pinned host) + pf_step({args.steps}) with per-step records + "
                             "pf_get_fields, host wall clock"},
             "gpu_launches": kernels_per_step * args.steps,
+            "kernel_variants": lib.pf_batch_variant(b).decode(),
         }
         if not args.no_cpu_baseline and ws == 1:
             v, cores, sample, n, dt = cpu_port_throughput(p, 20.0, 50)

@@ -7,7 +7,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -200,15 +202,17 @@ static const size_t kMaxSmem = 227 * 1024;
 
 static int validate(const pf_config* c) {
   if (!c) return fail(PF_EINVAL, "null config");
-  XKernels xk;
+  XKernels xv[kMaxVariants];
   YZKernels yk;
-  if (!get_x_kernels(c->nx, &xk)) return fail(PF_EINVAL, "Nx=%d not supported (16, 32, 64, 128, 256)", c->nx);
+  const int nxv = get_x_variants(c->nx, xv);
+  if (nxv == 0) return fail(PF_EINVAL, "Nx=%d not supported (16, 32, 64, 128, 256)", c->nx);
   if (!get_yz_kernels(c->ny, c->nz, &yk))
     return fail(PF_EINVAL, "(Ny, Nz)=(%d, %d) not supported by the fused FP32 path", c->ny, c->nz);
-  if (c->ny % xk.wy != 0) return fail(PF_EINVAL, "Ny=%d must be a multiple of %d for Nx=%d", c->ny, xk.wy, c->nx);
   if (c->var < 1 || c->var > 48) return fail(PF_EINVAL, "var=%d outside [1, 48]", c->var);
-  if (x_smem(c->nx, c->var + 1, xk.wy) > kMaxSmem)
-    return fail(PF_EINVAL, "var=%d too large for Nx=%d (shared memory)", c->var, c->nx);
+  bool fits = false;
+  for (int i = 0; i < nxv; ++i)
+    fits = fits || (c->ny % xv[i].wy == 0 && x_smem(c->nx, c->var + 1, xv[i].wy) <= kMaxSmem);
+  if (!fits) return fail(PF_EINVAL, "var=%d with Nx=%d, Ny=%d does not fit the x pass", c->var, c->nx, c->ny);
   if (c->mobility != PF_MOB_REFERENCE && c->mobility != PF_MOB_C1MC)
     return fail(PF_EINVAL, "unknown mobility form %d", c->mobility);
   if (!std::isfinite(c->t_step)) return fail(PF_EINVAL, "t_step not finite");
@@ -246,6 +250,7 @@ struct pf_batch {
   cudaGraphExec_t gexec = nullptr;
   std::vector<double> hdiag;
   std::vector<int> steps_done;
+  std::string variant;  // chosen kernel variants, for reports
 };
 
 struct pf_run {
@@ -277,16 +282,164 @@ static int enqueue_step(pf_batch* b, cudaStream_t s) {
   const Shape sh = b->tab.sh;
   const int R = b->nruns;
   const dim3 gx(b->Nz * (b->Ny / b->xk.wy), R);
-  b->xk.bulk<<<gx, 256, b->smem_x, s>>>(b->drp, sh);
+  b->xk.bulk<<<gx, b->xk.threads, b->smem_x, s>>>(b->drp, sh);
   int rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, R, s);
   if (rc) return rc;
   if (b->mob != MOB_CONST) {
-    b->xk.xj<<<gx, 256, b->smem_xj, s>>>(b->drp, sh);
+    b->xk.xj<<<gx, b->xk.threads, b->smem_xj, s>>>(b->drp, sh);
     rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, s);
     if (rc) return rc;
   }
   reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
   PF_CUDA(cudaGetLastError());
+  return PF_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Autotuner: time every compiled variant of the x and yz passes on this batch
+// (one warm-up + three timed launches each, on a synthetic non-zero state) and
+// keep the fastest.  The choice is cached per (shape, var, mobility, device)
+// for the life of the process, so every batch of a shape runs the same
+// kernels.  PFGPU_AUTOTUNE=0 keeps the default variants; PFGPU_X_VARIANT /
+// PFGPU_YZ_VARIANT force one.
+// ---------------------------------------------------------------------------
+__global__ void fill_kernel(float* p, size_t n, float v0, float v1) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = (i & 1) ? v1 : v0;
+}
+
+static std::mutex g_tune_mu;
+static std::map<std::string, std::pair<int, int>> g_tune_cache;
+
+static bool yz_ok(pf_batch* b, const YZKernels& k) {
+  if (k.smem > kMaxSmem) return false;
+  for (KernelFn f : {k.main, k.c2, k.imp}) {
+    if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem) != cudaSuccess)
+      return false;
+    if (k.cluster > 8 &&
+        cudaFuncSetAttribute((const void*)f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+      return false;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = k.cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(k.cluster * b->nF * b->Kx, 1);
+  cfg.blockDim = dim3(k.threads);
+  cfg.dynamicSmemBytes = k.smem;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int ncl = 0;
+  cudaError_t e = cudaOccupancyMaxActiveClusters(&ncl, (const void*)k.main, &cfg);
+  cudaGetLastError();
+  return e == cudaSuccess && ncl >= 1;
+}
+
+static bool x_ok(pf_batch* b, const XKernels& k) {
+  if (b->Ny % k.wy != 0) return false;
+  const size_t sm = x_smem(b->Nx, b->nF, k.wy);
+  if (sm > kMaxSmem) return false;
+  for (KernelFn f : {k.bulk, k.xj, k.imp, k.exp})
+    if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+      return false;
+  return true;
+}
+
+static void apply_variants(pf_batch* b, const XKernels& xk, const YZKernels& yk) {
+  b->xk = xk;
+  b->yk = yk;
+  b->smem_x = x_smem(b->Nx, b->nF, xk.wy);
+  b->smem_xj = x_smem(b->Nx, 1, xk.wy);
+  b->tab.sh.nblk_x = b->Nz * (b->Ny / xk.wy);
+  b->tab.sh.nblk_yz = yk.cluster * b->nF * b->Kx;
+  char buf[128];
+  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d yz:cluster=%d,threads=%d", xk.wy, xk.threads, yk.cluster, yk.threads);
+  b->variant = buf;
+}
+
+static int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  return v ? atoi(v) : dflt;
+}
+
+static int tune_batch(pf_batch* b) {
+  XKernels xv[kMaxVariants];
+  YZKernels yv[kMaxVariants];
+  const int nx = get_x_variants(b->Nx, xv), ny = get_yz_variants(b->Ny, b->Nz, yv);
+  std::vector<int> xs, ys;
+  for (int i = 0; i < nx; ++i)
+    if (x_ok(b, xv[i])) xs.push_back(i);
+  for (int i = 0; i < ny; ++i)
+    if (yz_ok(b, yv[i])) ys.push_back(i);
+  if (xs.empty()) return fail(PF_EINVAL, "no x-pass variant fits Nx=%d, Ny=%d, var=%d", b->Nx, b->Ny, b->V);
+  if (ys.empty()) return fail(PF_ECUDA, "no yz-pass variant can be scheduled for (%d, %d)", b->Ny, b->Nz);
+  char key[128];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d", b->Nx, b->Ny, b->Nz, b->V, b->mob, dev);
+  int bx = xs[0], by = ys[0];
+  const int fx = env_int("PFGPU_X_VARIANT", -1), fy = env_int("PFGPU_YZ_VARIANT", -1);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      bx = it->second.first;
+      by = it->second.second;
+    } else if (env_int("PFGPU_AUTOTUNE", 1) != 0 && (xs.size() > 1 || ys.size() > 1)) {
+      // synthetic non-zero state so that the bulk terms take their usual branches
+      const size_t nfin = (size_t)b->nF * b->Nx * b->Ny * b->Nz;
+      fill_kernel<<<(unsigned)((nfin + 255) / 256), 256, 0, b->stream>>>(b->fin, nfin, 0.3f, 0.7f);
+      apply_variants(b, xv[xs[0]], yv[ys[0]]);
+      const dim3 g1(b->Nz * (b->Ny / b->xk.wy), 1);
+      b->xk.imp<<<g1, b->xk.threads, b->smem_x, b->stream>>>(b->drp, b->tab.sh);
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      float best = 1e30f;
+      for (int i : xs) {
+        apply_variants(b, xv[i], yv[by]);
+        const dim3 gx(b->Nz * (b->Ny / b->xk.wy), b->nruns);
+        b->xk.bulk<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp, b->tab.sh);
+        cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < 3; ++r) b->xk.bulk<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp, b->tab.sh);
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (cudaGetLastError() == cudaSuccess && ms < best) { best = ms; bx = i; }
+      }
+      best = 1e30f;
+      for (int i : ys) {
+        apply_variants(b, xv[bx], yv[i]);
+        if (launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, b->nruns, b->stream)) { cudaGetLastError(); continue; }
+        cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < 3; ++r) launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, b->nruns, b->stream);
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (cudaGetLastError() == cudaSuccess && ms < best) { best = ms; by = i; }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      PF_CUDA(cudaStreamSynchronize(b->stream));
+      // leave a clean state behind
+      for (const RunParams& r : b->hrp) {
+        const size_t fbytes = (size_t)b->nF * b->Kx * b->Ny * b->Nz * sizeof(float2);
+        PF_CUDA(cudaMemsetAsync(r.Sk, 0, fbytes, b->stream));
+        PF_CUDA(cudaMemsetAsync(r.Sm, 0, fbytes, b->stream));
+        PF_CUDA(cudaMemsetAsync(r.D, 0, fbytes, b->stream));
+      }
+      PF_CUDA(cudaStreamSynchronize(b->stream));
+      g_tune_cache[key] = std::make_pair(bx, by);
+    }
+  }
+  if (fx >= 0 && fx < nx && x_ok(b, xv[fx])) bx = fx;
+  if (fy >= 0 && fy < ny && yz_ok(b, yv[fy])) by = fy;
+  apply_variants(b, xv[bx], yv[by]);
   return PF_OK;
 }
 
@@ -327,50 +480,12 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
     if (mob_mode(&cfgs[i]) != MOB_CONST) b->mob = mob_mode(&cfgs[i]);
   get_x_kernels(b->Nx, &b->xk);
   get_yz_kernels(b->Ny, b->Nz, &b->yk);
-  b->smem_x = x_smem(b->Nx, b->nF, b->xk.wy);
-  b->smem_xj = x_smem(b->Nx, 1, b->xk.wy);
   auto bail = [&](int rc) { destroy_batch(b); return rc; };
   cudaError_t e = cudaSetDevice(b->device);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "cudaSetDevice(%d): %s", b->device, cudaGetErrorString(e)));
   int rc = build_tables(b->Nx, b->Ny, b->Nz, b->tab);
   if (rc) return bail(rc);
   Shape& sh = b->tab.sh;
-  sh.nblk_x = b->Nz * (b->Ny / b->xk.wy);
-  sh.nblk_yz = b->yk.cluster * b->nF * b->Kx;
-
-  // kernel attributes (idempotent)
-  KernelFn xs[4] = {b->xk.bulk, b->xk.xj, b->xk.imp, b->xk.exp};
-  for (KernelFn k : xs) {
-    e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem_x);
-    if (e != cudaSuccess) return bail(fail(PF_ECUDA, "x-pass smem attribute: %s", cudaGetErrorString(e)));
-  }
-  for (KernelFn k : {b->yk.main, b->yk.c2, b->yk.imp}) {
-    e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->yk.smem);
-    if (e != cudaSuccess) return bail(fail(PF_ECUDA, "yz-pass smem attribute: %s", cudaGetErrorString(e)));
-    if (b->yk.cluster > 8) {
-      e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      if (e != cudaSuccess) return bail(fail(PF_ECUDA, "cluster attribute: %s", cudaGetErrorString(e)));
-    }
-  }
-  {
-    // the cluster shape must be schedulable on this device
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = b->yk.cluster;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(b->yk.cluster * b->nF * b->Kx, 1);
-    cfg.blockDim = dim3(b->yk.threads);
-    cfg.dynamicSmemBytes = b->yk.smem;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    int ncl = 0;
-    e = cudaOccupancyMaxActiveClusters(&ncl, (const void*)b->yk.main, &cfg);
-    if (e != cudaSuccess || ncl < 1)
-      return bail(fail(PF_ECUDA, "yz cluster of %d CTAs with %zu B smem cannot be scheduled: %s", b->yk.cluster,
-                       b->yk.smem, cudaGetErrorString(e)));
-  }
 
   // buffers
   const size_t plane = (size_t)b->Ny * b->Nz;
@@ -382,8 +497,10 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   const size_t szS = align(b->nF * fieldc * sizeof(float2));
   const size_t szMob = var ? align(ncell * sizeof(float)) : 0;
   const size_t szJ = var ? align(fieldc * sizeof(float2)) : 0;  // J~ scratch
-  const size_t szPx = align((size_t)XD_COUNT * sh.nblk_x * sizeof(double));
-  const size_t szPyz = align((size_t)sh.nblk_yz * sizeof(double));
+  // partial arrays sized for every variant (at least one y row per x-pass
+  // block, at most 16 CTAs per yz cluster)
+  const size_t szPx = align((size_t)XD_COUNT * b->Nz * b->Ny * sizeof(double));
+  const size_t szPyz = align((size_t)16 * b->nF * b->Kx * sizeof(double));
   const size_t szDiag = align((size_t)b->ring * DR_COUNT * sizeof(double));
   const size_t szCnt = 256;
   const size_t per_run = 3 * szS + szMob + szJ + szPx + szPyz + szDiag + szCnt;
@@ -436,6 +553,9 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream: %s", cudaGetErrorString(e)));
 
+  rc = tune_batch(b);
+  if (rc) return bail(rc);
+
   // capture one step as a CUDA graph
   cudaGraph_t g = nullptr;
   e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
@@ -461,7 +581,7 @@ static int batch_set_fields(pf_batch* b, int run, const double* phi, const doubl
   PF_CUDA(cudaMemcpyAsync(dcon, con, ncell * sizeof(double), cudaMemcpyHostToDevice, b->stream));
   aos_to_soa_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, b->stream>>>(dphi, dcon, b->fin, b->V, ncell);
   const dim3 gx(b->Nz * (b->Ny / b->xk.wy), 1);
-  b->xk.imp<<<gx, 256, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
+  b->xk.imp<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
   int rc = launch_yz(b, b->yk.imp, b->nF * b->Kx, b->drp + run, 1, b->stream);
   if (rc) return rc;
   PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, sizeof(int), b->stream));
@@ -478,7 +598,7 @@ static int batch_get_fields(pf_batch* b, int run, double* phi, double* con) {
   double* dphi = b->dstage;
   double* dcon = b->dstage + (size_t)b->V * ncell;
   const dim3 gx(b->Nz * (b->Ny / b->xk.wy), 1);
-  b->xk.exp<<<gx, 256, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
+  b->xk.exp<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
   soa_to_aos_kernel<<<(unsigned)((ncell + 255) / 256), 256, 0, b->stream>>>(b->fin, dphi, dcon, b->V, ncell);
   PF_CUDA(cudaGetLastError());
   PF_CUDA(cudaMemcpyAsync(phi, dphi, (size_t)b->V * ncell * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
@@ -622,6 +742,7 @@ int pf_batch_enqueue(pf_batch* b, int nsteps) {
   return PF_OK;
 }
 void* pf_batch_stream(pf_batch* b) { return b ? (void*)b->stream : nullptr; }
+const char* pf_batch_variant(pf_batch* b) { return b ? b->variant.c_str() : ""; }
 pf_batch* pf_run_batch(pf_run* r) { return r ? r->b : nullptr; }
 // Launch the x pass / yz pass alone (kernel timing); returns PF_OK.
 int pf_batch_enqueue_phase(pf_batch* b, int phase) {
@@ -629,7 +750,7 @@ int pf_batch_enqueue_phase(pf_batch* b, int phase) {
   const Shape sh = b->tab.sh;
   const dim3 gx(b->Nz * (b->Ny / b->xk.wy), b->nruns);
   if (phase == 0) {
-    b->xk.bulk<<<gx, 256, b->smem_x, b->stream>>>(b->drp, sh);
+    b->xk.bulk<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp, sh);
   } else {
     int rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, b->nruns, b->stream);
     if (rc) return rc;

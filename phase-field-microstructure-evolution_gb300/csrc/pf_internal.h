@@ -10,11 +10,14 @@ namespace pf {
 
 typedef void (*KernelFn)(const RunParams*, const Shape);
 
+// One compiled variant of the x pass (all four modes) ...
 struct XKernels {
   KernelFn bulk, xj, imp, exp;
-  int wy;  // y rows per CTA
+  int wy;       // y rows per CTA
+  int threads;  // threads per CTA
 };
 
+// ... and of the yz pass (all three modes).
 struct YZKernels {
   KernelFn main, c2, imp;  // modes YZ_MAIN, YZ_C2, YZ_IMPORT
   int cluster;   // CTAs per plane
@@ -22,15 +25,39 @@ struct YZKernels {
   size_t smem;   // dynamic shared memory per CTA
 };
 
-// implemented in pf_x.cu / pf_yz_*.cu
-bool get_x_kernels(int nx, XKernels* out);
-bool get_yz_kernels_small(int ny, int nz, YZKernels* out);
-bool get_yz_kernels_128(int ny, int nz, YZKernels* out);
-bool get_yz_kernels_256(int ny, int nz, YZKernels* out);
+// Variant lists: each translation unit appends the variants it compiled for a
+// shape to `out` (room for kMaxVariants entries) and returns the new count.  The first variant of a shape is its
+// default; the run-creation autotuner times the others.
+constexpr int kMaxVariants = 16;
+int x_variants_a(int nx, XKernels* out, int n);
+int yz_variants_small(int ny, int nz, YZKernels* out, int n);
+int yz_variants_128a(int ny, int nz, YZKernels* out, int n);
+int yz_variants_128b(int ny, int nz, YZKernels* out, int n);
+int yz_variants_256a(int ny, int nz, YZKernels* out, int n);
+int yz_variants_256b(int ny, int nz, YZKernels* out, int n);
 
+inline int get_x_variants(int nx, XKernels* out) { return x_variants_a(nx, out, 0); }
+inline int get_yz_variants(int ny, int nz, YZKernels* out) {
+  int n = 0;
+  n = yz_variants_small(ny, nz, out, n);
+  n = yz_variants_128a(ny, nz, out, n);
+  n = yz_variants_128b(ny, nz, out, n);
+  n = yz_variants_256a(ny, nz, out, n);
+  n = yz_variants_256b(ny, nz, out, n);
+  return n;
+}
+// default (first) variant of a shape; `out` receives one entry
+inline bool get_x_kernels(int nx, XKernels* out) {
+  XKernels v[kMaxVariants];
+  if (get_x_variants(nx, v) == 0) return false;
+  *out = v[0];
+  return true;
+}
 inline bool get_yz_kernels(int ny, int nz, YZKernels* out) {
-  return get_yz_kernels_small(ny, nz, out) || get_yz_kernels_128(ny, nz, out) ||
-         get_yz_kernels_256(ny, nz, out);
+  YZKernels v[kMaxVariants];
+  if (get_yz_variants(ny, nz, v) == 0) return false;
+  *out = v[0];
+  return true;
 }
 
 // x-pass shared memory for nF fields

@@ -918,4 +918,237 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   }
 }
 
+// ---------------------------------------------------------------------------
+// Single-CTA yz pass for planes that fit one CTA's shared memory: the plane
+// stays in one buffer U[z][phys_y(y)] (row pitch PY, odd); y transforms run
+// along rows, z transforms down columns (consecutive threads take consecutive
+// y positions, so column accesses are conflict-free).  No re-layout, no
+// cluster.  Same k-space position order as the cluster kernel.
+// ---------------------------------------------------------------------------
+template <int NY, int NZ>
+struct YZ1 {
+  static constexpr int PY = Line<NY>::PITCH;
+  static constexpr size_t SMEM = (size_t)NZ * PY * sizeof(float2);
+};
+
+// column pass A (forward or inverse) over the NY y positions
+template <int NY, int NZ, int T, bool INV>
+__device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
+  constexpr int N1 = Line<NZ>::N1, N2 = Line<NZ>::N2, PY = YZ1<NY, NZ>::PY;
+  constexpr int ITEMS = NY * N1, ITER = (ITEMS + T - 1) / T;
+#pragma unroll 1
+  for (int j = 0; j < ITER; ++j) {
+    const int it = threadIdx.x + j * T;
+    if (ITEMS % T != 0 && it >= ITEMS) break;
+    const int yp = it % NY, n1 = it / NY;
+    float2* p = U + n1 * PY + Line<NY>::phys(yp);
+    float2 v[N2];
+    if (!INV) {
+#pragma unroll
+      for (int n2 = 0; n2 < N2; ++n2) v[n2] = p[n2 * N1 * PY];
+      Dft<N2>::fwd(v);
+#pragma unroll
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], __ldg(tw + n1 * k2));
+    } else {
+      v[0] = p[0];
+#pragma unroll
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * N1 * PY], __ldg(tw + n1 * k2));
+      dft_inv<N2>(v);
+    }
+#pragma unroll
+    for (int k = 0; k < N2; ++k) p[k * N1 * PY] = v[k];
+  }
+}
+
+template <int NY, int NZ, int T, int MODE>
+__global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ runs, const Shape sh) {
+  using LY = Line<NY>;
+  using LZ = Line<NZ>;
+  constexpr int N1y = LY::N1, N2y = LY::N2, N1z = LZ::N1, N2z = LZ::N2;
+  constexpr int PY = YZ1<NY, NZ>::PY;
+  static_assert(T % N1y == 0 && T % N2y == 0, "thread count");
+  extern __shared__ float2 U[];
+  __shared__ double red[T / 32];
+  const RunParams& rp = runs[blockIdx.y];
+  const int p = blockIdx.x;
+  const int Kx = sh.Kx;
+  const int f = (MODE == YZ_C2) ? rp.V : p / Kx;
+  const int kx = p - (p / Kx) * Kx;
+  const size_t plane_elems = (size_t)NZ * NY;
+  const size_t poff = ((size_t)f * Kx + kx) * plane_elems;
+  const bool is_c = (f == rp.V);
+  const bool var_c = (MODE == YZ_MAIN) && is_c && rp.mobility != MOB_CONST;
+
+  // 1. forward y transform of all NZ rows, first pass straight from global
+  {
+    const float2* src = (MODE == YZ_MAIN) ? rp.D + poff : (MODE == YZ_C2 ? rp.J + kx * plane_elems : rp.Sm + poff);
+    const int n1 = threadIdx.x % N1y;
+    float2 wt[N2y];
+#pragma unroll
+    for (int k2 = 1; k2 < N2y; ++k2) wt[k2] = __ldg(sh.twY + n1 * k2);
+    constexpr int ITEMS = NZ * N1y, ITER = (ITEMS + T - 1) / T;
+#pragma unroll 2
+    for (int j = 0; j < ITER; ++j) {
+      const int it = threadIdx.x + j * T;
+      if (ITEMS % T != 0 && it >= ITEMS) break;
+      const int z = it / N1y;
+      const float2* s = src + (size_t)z * NY + n1;
+      float2 v[N2y];
+#pragma unroll
+      for (int n2 = 0; n2 < N2y; ++n2) v[n2] = __ldg(s + n2 * N1y);
+      Dft<N2y>::fwd(v);
+      float2* d = U + z * PY + n1;
+      d[0] = v[0];
+#pragma unroll
+      for (int k2 = 1; k2 < N2y; ++k2) d[k2 * (N1y + 1)] = cmul(v[k2], wt[k2]);
+    }
+  }
+  __syncthreads();
+  passB<NY, NZ, PY, T, false>(U);
+  __syncthreads();
+  colA<NY, NZ, T, false>(U, sh.twZ);
+  __syncthreads();
+
+  // 2. last forward z pass, pointwise k-space update, first inverse z pass
+  const float inv_nyz = 1.0f / (float)(NY * NZ);
+  const float qx2 = sh.qx2[kx], qx4 = sh.qx4[kx], qnx = sh.qnx[kx];
+  const float wkx = (kx == 0 || 2 * kx == sh.Nx) ? 1.0f : 2.0f;
+  float fint = 0.f;
+  {
+    constexpr int ITEMS = NY * N2z, ITER = (ITEMS + T - 1) / T;
+#pragma unroll 1
+    for (int j = 0; j < ITER; ++j) {
+      const int it = threadIdx.x + j * T;
+      if (ITEMS % T != 0 && it >= ITEMS) break;
+      const int yp = it % NY, k2 = it / NY;
+      const int ky = LY::freq_of_pos(yp);
+      const float qy2 = __ldg(sh.qy2 + ky), qy4 = __ldg(sh.qy4 + ky), qn_y = __ldg(sh.qny + ky);
+      float2* pc = U + (k2 * N1z) * PY + LY::phys(yp);
+      float2* gk = rp.Sk + poff + (size_t)yp * NZ + k2 * N1z;  // k-space state run
+      float2 d[N1z], u[N1z];
+      if (MODE != YZ_IMPORT) {
+#pragma unroll
+        for (int k1 = 0; k1 < N1z; k1 += 2) {
+          const float4 t = *reinterpret_cast<const float4*>(gk + k1);
+          u[k1] = make_float2(t.x, t.y);
+          u[k1 + 1] = make_float2(t.z, t.w);
+        }
+      }
+#pragma unroll
+      for (int k1 = 0; k1 < N1z; ++k1) d[k1] = pc[k1 * PY];
+      Dft<N1z>::fwd(d);
+#pragma unroll
+      for (int k1 = 0; k1 < N1z; ++k1) {
+        const int kz = k2 + N2z * k1;
+        const float2 dd = make_float2(d[k1].x * inv_nyz, d[k1].y * inv_nyz);  // normalised D_hat
+        if (MODE == YZ_IMPORT) {
+          u[k1] = dd;
+          continue;
+        }
+        const float2 uu = u[k1];
+        const float q2 = qx2 + qy2 + __ldg(sh.qz2 + kz);
+        const float qn_z = __ldg(sh.qnz + kz);
+        if (MODE == YZ_MAIN) {
+          const float kn2 = qnx * qnx + qn_y * qn_y + qn_z * qn_z;
+          fint = fmaf(kn2, uu.x * uu.x + uu.y * uu.y, fint);
+          if (!is_c) {
+            // AC (:1015-1024): u += (-L dt kappa q^2 u - L dt D) / (1 + L kappa dt q^2)
+            const float lk = rp.L * rp.dt;
+            const float inv = 1.0f / fmaf(lk * rp.kappa_phi, q2, 1.0f);
+            const float m1 = -lk * rp.kappa_phi * q2 * inv;
+            const float m2 = -lk * inv;
+            u[k1] = make_float2(uu.x + fmaf(m1, uu.x, m2 * dd.x), uu.y + fmaf(m1, uu.y, m2 * dd.y));
+          } else {
+            // CH (:976-983): c += (-D dt kappa_c K4 c + D K2 dt mu) / (1 + D dt kappa_c K4), K2 = -q^2
+            const float q4 = qx4 + qy4 + __ldg(sh.qz4 + kz);
+            const float dm = rp.D_L * rp.dt;
+            const float inv = 1.0f / fmaf(dm * rp.kappa_c, q4, 1.0f);
+            const float m1 = -dm * rp.kappa_c * q4 * inv;
+            const float m2 = -dm * q2 * inv;
+            u[k1] = make_float2(uu.x + fmaf(m1, uu.x, m2 * dd.x), uu.y + fmaf(m1, uu.y, m2 * dd.y));
+            if (var_c) {
+              // J_hat = G mu_hat - kappa_c c_hat K3 (:932-935), G = i g, K3 = i k3
+              const float g = qnx + qn_y + qn_z;
+              const float k3 = -(qnx * qx2 + qn_y * qy2 + qn_z * __ldg(sh.qz2 + kz));
+              d[k1] = cmul_pi(make_float2(g * dd.x - rp.kappa_c * k3 * uu.x, g * dd.y - rp.kappa_c * k3 * uu.y));
+            }
+          }
+        } else {
+          // C2: c += dt G J'_hat / (1 + D dt kappa_c K4)  (:976)
+          const float q4 = qx4 + qy4 + __ldg(sh.qz4 + kz);
+          const float dm = rp.D_L * rp.dt;
+          const float g = qnx + qn_y + qn_z;
+          const float sgl = rp.dt * g / fmaf(dm * rp.kappa_c, q4, 1.0f);
+          u[k1] = cadd(uu, cmul_pi(make_float2(dd.x * sgl, dd.y * sgl)));
+        }
+      }
+#pragma unroll
+      for (int k1 = 0; k1 < N1z; k1 += 2)
+        *reinterpret_cast<float4*>(gk + k1) = make_float4(u[k1].x, u[k1].y, u[k1 + 1].x, u[k1 + 1].y);
+      if (MODE != YZ_IMPORT) {
+        if (var_c) {
+          dft_inv<N1z>(d);
+#pragma unroll
+          for (int k1 = 0; k1 < N1z; ++k1) pc[k1 * PY] = d[k1];
+        } else {
+          dft_inv<N1z>(u);
+#pragma unroll
+          for (int k1 = 0; k1 < N1z; ++k1) pc[k1 * PY] = u[k1];
+        }
+      }
+    }
+  }
+  if (MODE == YZ_IMPORT) return;
+  __syncthreads();
+  colA<NY, NZ, T, true>(U, sh.twZ);
+  __syncthreads();
+  passB<NY, NZ, PY, T, true>(U);
+  __syncthreads();
+
+  // 3. last inverse y pass straight to the mixed-space output
+  {
+    const bool real_plane = (kx == 0) || (2 * kx == sh.Nx);  // the x-DFT of real data is real there
+    float2* dst = var_c ? rp.J + kx * plane_elems : rp.Sm + poff;
+    const int n1 = threadIdx.x % N1y;
+    float2 wt[N2y];
+#pragma unroll
+    for (int k2 = 1; k2 < N2y; ++k2) wt[k2] = __ldg(sh.twY + n1 * k2);
+    constexpr int ITEMS = NZ * N1y, ITER = (ITEMS + T - 1) / T;
+#pragma unroll 2
+    for (int j = 0; j < ITER; ++j) {
+      const int it = threadIdx.x + j * T;
+      if (ITEMS % T != 0 && it >= ITEMS) break;
+      const int z = it / N1y;
+      const float2* sp = U + z * PY + n1;
+      float2 v[N2y];
+      v[0] = sp[0];
+#pragma unroll
+      for (int k2 = 1; k2 < N2y; ++k2) v[k2] = cmulc(sp[k2 * (N1y + 1)], wt[k2]);
+      dft_inv<N2y>(v);
+      float2* o = dst + (size_t)z * NY + n1;
+#pragma unroll
+      for (int n2 = 0; n2 < N2y; ++n2) {
+        float2 x = v[n2];
+        if (real_plane && !var_c) x.y = 0.f;
+        o[n2 * N1y] = x;
+      }
+    }
+  }
+
+  if (MODE == YZ_MAIN) {
+    double v = warp_sum((double)fint);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0;
+#pragma unroll
+      for (int q = 0; q < T / 32; ++q) s += red[q];
+      const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
+      const double n3 = (double)sh.Nx * NY * NZ;
+      rp.part_yz[blockIdx.x] = s * wkx * 0.5 * kap * n3;
+    }
+  }
+}
+
 }  // namespace pf

@@ -1,28 +1,38 @@
 // Instantiations of the x pass (fused bulk kernel and x-direction transforms)
-// for the supported Nx.  y rows per CTA (WY) are chosen so that a CTA has
-// 128-256 two-cell work items and global rows are read in >= 32-byte runs.
+// for the supported Nx: several (rows per CTA, threads per CTA) variants per
+// size; the first one is the default, the autotuner picks among them.
 #include "pf_internal.h"
 
 namespace pf {
 
-template <int NX, int WY>
-static void fill(XKernels* k) {
-  k->bulk = x_pass_kernel<NX, WY, 256, MODE_BULK>;
-  k->xj = x_pass_kernel<NX, WY, 256, MODE_XJ>;
-  k->imp = x_pass_kernel<NX, WY, 256, MODE_IMPORT>;
-  k->exp = x_pass_kernel<NX, WY, 256, MODE_EXPORT>;
-  k->wy = WY;
+template <int NX, int WY, int T>
+static int add(XKernels* out, int n) {
+  if (n >= kMaxVariants) return n;
+  XKernels& k = out[n];
+  k.bulk = x_pass_kernel<NX, WY, T, MODE_BULK>;
+  k.xj = x_pass_kernel<NX, WY, T, MODE_XJ>;
+  k.imp = x_pass_kernel<NX, WY, T, MODE_IMPORT>;
+  k.exp = x_pass_kernel<NX, WY, T, MODE_EXPORT>;
+  k.wy = WY;
+  k.threads = T;
+  return n + 1;
 }
 
-bool get_x_kernels(int nx, XKernels* out) {
+int x_variants_a(int nx, XKernels* out, int n) {
   switch (nx) {
-    case 16: fill<16, 16>(out); return true;
-    case 32: fill<32, 16>(out); return true;
-    case 64: fill<64, 8>(out); return true;
-    case 128: fill<128, 8>(out); return true;
-    case 256: fill<256, 4>(out); return true;
-    default: return false;
+    case 16: n = add<16, 16, 256>(out, n); break;
+    case 32: n = add<32, 16, 256>(out, n); n = add<32, 8, 128>(out, n); break;
+    case 64: n = add<64, 8, 256>(out, n); n = add<64, 16, 256>(out, n); n = add<64, 4, 128>(out, n); break;
+    case 128:
+      n = add<128, 8, 256>(out, n);
+      n = add<128, 4, 256>(out, n);
+      n = add<128, 4, 128>(out, n);
+      n = add<128, 16, 256>(out, n);
+      break;
+    case 256: n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n); break;
+    default: break;
   }
+  return n;
 }
 
 }  // namespace pf

@@ -98,6 +98,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_batch_enqueue": (C.c_int, [C.c_void_p, C.c_int]),
         "pf_batch_enqueue_phase": (C.c_int, [C.c_void_p, C.c_int]),
         "pf_batch_stream": (C.c_void_p, [C.c_void_p]),
+        "pf_batch_variant": (C.c_char_p, [C.c_void_p]),
         "pf_run_batch": (C.c_void_p, [C.c_void_p]),
         "f_trans_": (None, [dp, dp, ip, ip, ip, ip, ip, ip, ip]),
         "inv_trans_": (None, [dp, dp, ip, ip, ip, ip]),

@@ -70,3 +70,15 @@ def test_library_ics_match_oracle(pkg, oracle, kind):
         a = pkg.ic_voronoi(p, 4, 7, 0.01, 0.5, 0.02)
         b = oracle.ic_voronoi(p, 4, 7, 0.01, 0.5, 0.02)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_create_without_gpu_fails_cleanly(pkg, oracle):
+    """On a host without a usable GPU, pf_create reports a CUDA error (no
+    crash, no CPU fallback)."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(pkg.PFError) as e:
+        pkg.Run(oracle.Params(32, 32, 32, 4))
+    assert e.value.code == -2
