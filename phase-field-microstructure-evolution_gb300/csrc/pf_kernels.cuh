@@ -121,16 +121,18 @@ __device__ __forceinline__ void post_pair(float2 zk, float2 zm, float2 wk, float
   xm = cscale(cadd(cconj(s), cmul_mi(cmul(d2, wm))), h);
 }
 
-// pass A over a runtime number of lines (pitch P, T threads)
+// pass A over a runtime number of lines (pitch P, T threads).  A warp takes 32
+// consecutive lines at one column n1: with an odd pitch those 32 accesses hit
+// distinct bank pairs.
 template <int L, int P, int T, bool INV>
 __device__ __forceinline__ void passA_rt(float2* buf, int NL, const float2* __restrict__ tw) {
   constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
-  static_assert(T % N1 == 0, "threads must be a multiple of N1");
-  const int n1 = threadIdx.x % N1;
-  float2 w[N2];
-#pragma unroll
-  for (int k2 = 1; k2 < N2; ++k2) w[k2] = __ldg(tw + n1 * k2);
-  for (int l = threadIdx.x / N1; l < NL; l += T / N1) {
+  const int nlb = (NL + 31) >> 5;  // groups of 32 lines
+  const int items = nlb * 32 * N1;
+  for (int it = threadIdx.x; it < items; it += T) {
+    const int lo = it & 31, rest = it >> 5;
+    const int n1 = rest % N1, l = (rest / N1) * 32 + lo;
+    if (l >= NL) continue;
     float2* p = buf + l * P + n1;
     float2 v[N2];
     if (!INV) {
@@ -138,11 +140,11 @@ __device__ __forceinline__ void passA_rt(float2* buf, int NL, const float2* __re
       for (int n2 = 0; n2 < N2; ++n2) v[n2] = p[n2 * (N1 + 1)];
       Dft<N2>::fwd(v);
 #pragma unroll
-      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], w[k2]);
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], __ldg(tw + n1 * k2));
     } else {
       v[0] = p[0];
 #pragma unroll
-      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * (N1 + 1)], w[k2]);
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * (N1 + 1)], __ldg(tw + n1 * k2));
       dft_inv<N2>(v);
     }
 #pragma unroll
@@ -431,9 +433,12 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
     }
   } else {
     // 1. inverse x transform: global half spectrum -> pre-processing -> pass B'
+    // a warp covers consecutive (y row, field) lines at one run pair: the
+    // global reads are y-contiguous and the line offsets hit distinct banks
     for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
-      const int yy = it % WY, r = it / WY, pr = r % NP, f = r / NP;
-      x_inv_runs<M>(src + f * fstride + row_off + yy, plane, smem + (f * WY + yy) * PM, pr, sh.twN);
+      const int l = it % (nF * WY), pr = it / (nF * WY);
+      const int f = l / WY, yy = l - f * WY;
+      x_inv_runs<M>(src + f * fstride + row_off + yy, plane, smem + l * PM, pr, sh.twN);
     }
     __syncthreads();
     passA_rt<M, PM, T, true>(smem, nF * WY, sh.twM);
@@ -485,8 +490,9 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
   float2* __restrict__ dst = (MODE == MODE_BULK) ? rp.D : (MODE == MODE_XJ ? rp.J : rp.Sm);
   const float scale = 1.0f / (float)NX;
   for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
-    const int yy = it % WY, r = it / WY, pr = r % NP, f = r / NP;
-    x_fwd_runs<M>(dst + f * fstride + row_off + yy, plane, smem + (f * WY + yy) * PM, pr, scale, sh.twN);
+    const int l = it % (nF * WY), pr = it / (nF * WY);
+    const int f = l / WY, yy = l - f * WY;
+    x_fwd_runs<M>(dst + f * fstride + row_off + yy, plane, smem + l * PM, pr, scale, sh.twN);
   }
 
   if (MODE != MODE_BULK) return;
