@@ -298,7 +298,7 @@ static int enqueue_step(pf_batch* b, cudaStream_t s) {
 
 // ---------------------------------------------------------------------------
 // Autotuner: time every compiled variant of the x and yz passes on this batch
-// (one warm-up + three timed launches each, on a synthetic non-zero state) and
+// (whole steps, three interleaved rounds, on a synthetic non-zero state) and
 // keep the fastest.  The choice is cached per (shape, var, mobility, device)
 // for the life of the process, so every batch of a shape runs the same
 // kernels.  PFGPU_AUTOTUNE=0 keeps the default variants; PFGPU_X_VARIANT /
@@ -398,31 +398,35 @@ static int tune_batch(pf_batch* b) {
       cudaEvent_t e0, e1;
       cudaEventCreate(&e0);
       cudaEventCreate(&e1);
-      float best = 1e30f;
-      for (int i : xs) {
-        apply_variants(b, xv[i], yv[by]);
-        const dim3 gx(b->Nz * (b->Ny / b->xk.wy), b->nruns);
-        b->xk.bulk<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp, b->tab.sh);
+      // Whole steps are timed (kernel order and L2 contents as in the run),
+      // in interleaved rounds, keeping the best time per variant: first the
+      // x variants with the default yz variant, then the yz variants.
+      const int ROUNDS = 3, REPS = 3;
+      auto time_steps = [&](float& out) {
+        if (enqueue_step(b, b->stream)) { cudaGetLastError(); return; }
         cudaEventRecord(e0, b->stream);
-        for (int r = 0; r < 3; ++r) b->xk.bulk<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp, b->tab.sh);
+        for (int r = 0; r < REPS; ++r) enqueue_step(b, b->stream);
         cudaEventRecord(e1, b->stream);
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (cudaGetLastError() == cudaSuccess && ms < best) { best = ms; bx = i; }
-      }
-      best = 1e30f;
-      for (int i : ys) {
-        apply_variants(b, xv[bx], yv[i]);
-        if (launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, b->nruns, b->stream)) { cudaGetLastError(); continue; }
-        cudaEventRecord(e0, b->stream);
-        for (int r = 0; r < 3; ++r) launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, b->nruns, b->stream);
-        cudaEventRecord(e1, b->stream);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (cudaGetLastError() == cudaSuccess && ms < best) { best = ms; by = i; }
-      }
+        if (cudaGetLastError() == cudaSuccess) out = std::min(out, ms);
+      };
+      std::vector<float> tx(nx, 1e30f), ty(ny, 1e30f);
+      for (int round = 0; round < ROUNDS; ++round)
+        for (int i : xs) {
+          apply_variants(b, xv[i], yv[by]);
+          time_steps(tx[i]);
+        }
+      for (int i : xs)
+        if (tx[i] < tx[bx]) bx = i;
+      for (int round = 0; round < ROUNDS; ++round)
+        for (int i : ys) {
+          apply_variants(b, xv[bx], yv[i]);
+          time_steps(ty[i]);
+        }
+      for (int i : ys)
+        if (ty[i] < ty[by]) by = i;
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       PF_CUDA(cudaStreamSynchronize(b->stream));
@@ -432,6 +436,7 @@ static int tune_batch(pf_batch* b) {
         PF_CUDA(cudaMemsetAsync(r.Sk, 0, fbytes, b->stream));
         PF_CUDA(cudaMemsetAsync(r.Sm, 0, fbytes, b->stream));
         PF_CUDA(cudaMemsetAsync(r.D, 0, fbytes, b->stream));
+        PF_CUDA(cudaMemsetAsync(r.counter, 0, sizeof(int), b->stream));
       }
       PF_CUDA(cudaStreamSynchronize(b->stream));
       g_tune_cache[key] = std::make_pair(bx, by);
