@@ -147,6 +147,24 @@ typedef struct pf_ran2_state {
 void pf_ran2_init(pf_ran2_state* st);
 double pf_ran2(pf_ran2_state* st, int* idum);
 
+/* ---- diagnostics without allocation ---------------------------------------
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory (their memory belongs to another runtime's pool, they run under a
+ * fixed memory cap, or they may not call cudaMalloc where they are): the
+ * f_eta, f_ch, mass, c_min, c_max, phi_min and phi_P_max of the pf_step record
+ * (src/var_diff.f90:685-759, :1076-1102), computed from fields the caller
+ * already holds on the current device, with no allocation.
+ *   fields: float [var+1][nz][ny][nx] device memory, phi_1..phi_var then c;
+ *   out:    host record; f_int and e_tot are NaN (they need the transforms);
+ *   stream: cudaStream_t or NULL; the call waits for its own work.
+ * Scratch is a fixed 512 KiB __device__ array present on every GPU that loads
+ * the library until the process exits; grids above PF_NOALLOC_MAX_CELLS are
+ * rejected with PF_EINVAL.  The first call on a device looks up the scratch
+ * address there: make it before any stream capture.  All calls share the
+ * scratch, so calls that overlap on the GPU race. */
+#define PF_NOALLOC_MAX_CELLS (256 * 256 * 256)
+int pf_diag_fields_noalloc(const pf_config* cfg, const float* fields, pf_diag* out, void* stream);
+
 /* Seeded starts (host only).  Draw order z, y, x (x fastest), per cell var phi
  * values then c, U(-a, a) = a (2 r - 1), r from ran_2 with idum = -(seed+1).
  * pf_ic_voronoi first draws n_grains points (Nx r, Ny r, Nz r); every cell
