@@ -165,6 +165,75 @@ double pf_ran2(pf_ran2_state* st, int* idum);
 #define PF_NOALLOC_MAX_CELLS (256 * 256 * 256)
 int pf_diag_fields_noalloc(const pf_config* cfg, const float* fields, pf_diag* out, void* stream);
 
+/* ---- input.txt, restart files and the reference's starts (host only) -----
+ * The values of src/var_diff.f90:104-121, read with Fortran list-directed
+ * rules: one READ per record, blanks or commas between values, r*c repeats,
+ * quoted strings, '/' ends a record early (the items after it keep their
+ * previous value: set_mask bit b says which group was read), a record may
+ * continue on following lines.  Lines after `start` may hold key=value pairs
+ * that the reference ignores: seed, n_grains, amp_phi, amp_c, c0 (for the
+ * 'noise' and 'voronoi' starts), mobility (reference|c1mc), precision (32|64),
+ * microstructure (the 'polycryst' file; the reference opens a fixed path). */
+typedef struct pf_input {
+  int nrun, ppt_int;                       /* bits 0, 1 */
+  int ppt_rad[3], N_step, ifreq;           /* bits 2, 3, 4 */
+  int i_ppt, j_ppt, k_ppt, iseed;          /* bits 5, 6 */
+  int grn_rad, num_ppt;                    /* bits 7, 8 */
+  double c_mat, c_ppt;                     /* bits 9, 10 */
+  int Nx, Ny, Nz, var;                     /* bits 11, 12 */
+  double dx, dy, dz, t_step;               /* bits 13, 14 */
+  double grad_coeff_phi, grad_coeff_c, D_S, D_L, D_gb, mob_phi; /* bits 15-20 */
+  double sigma_1, sigma_2;                 /* bit 21 */
+  double am, ap, con_0_mat, con_0_ppt;     /* bits 22, 23 */
+  double gb_force;                         /* bit 24 */
+  int ndim, dims[2];                       /* bits 25, 26 */
+  char start[16];                          /* bit 27 (character*10 in the reference) */
+  unsigned long long set_mask;
+  /* key=value extensions */
+  int seed, n_grains, mobility, precision; /* precision 0: fused FP32 where supported */
+  double amp_phi, amp_c, c0;
+  char microstructure[256];
+} pf_input;
+
+/* Message of the last failed pf_read_input / pf_*data_save / pf_ic_* call. */
+const char* pf_io_last_error(void);
+/* Read input.txt (src/var_diff.f90:104-121); nprocs fills dims when ndim = 1. */
+int pf_read_input(const char* path, int nprocs, pf_input* in);
+/* pf_config of the step from an input record (device 0). */
+void pf_input_to_config(const pf_input* in, pf_config* cfg);
+
+/* data_save.NNNN / data_rerun.NNNN (src/var_diff.f90:1134-1140, :453-458):
+ * Fortran unformatted sequential, two records "ist, ien" (6 INTEGER*4) and
+ * "phi, con" (REAL*8, phi(var,x,y,z) then con(x,y,z)), gfortran record
+ * markers (4-byte lengths; sub-records above 2^31-9 bytes), one rank. */
+int pf_write_data_save(const char* path, const pf_config* cfg, const double* phi_aos, const double* con);
+int pf_read_data_save(const char* path, const pf_config* cfg, double* phi_aos, double* con);
+
+/* The reference's starts, one rank, phi(var,x,y,z) / con(x,y,z) REAL*8.
+ * 'circle' (src/var_diff.f90:373-449) draws from ran_2 with *idum and *st and
+ * leaves both advanced, as the later precipitate insertion continues them. */
+int pf_ic_circle(const pf_config* cfg, int grn_rad, const int* ppt_rad, int num_ppt, int* idum, double c_mat,
+                 double con_0_ppt, pf_ran2_state* st, double* phi_aos, double* con);
+/* 'plane' (src/var_diff.f90:252-371) */
+int pf_ic_plane(const pf_config* cfg, const int* ppt_rad, int i_ppt, int j_ppt, int k_ppt, double c_mat,
+                double* phi_aos, double* con);
+/* 'polycryst' (src/var_diff.f90:232-250): Nx*Ny*Nz text lines "i j k ivar" */
+int pf_ic_polycryst(const pf_config* cfg, const char* path, double c_mat, double* phi_aos, double* con);
+/* Precipitates inserted at step ppt_int (src/var_diff.f90:479-554). */
+int pf_insert_precipitates(const pf_config* cfg, const int* ppt_rad, int num_ppt, int* idum, pf_ran2_state* st,
+                           double* phi_aos);
+/* Fortran Ew.d edit of x into out (w+1 bytes), e.g. the e15.7 of summary.dat. */
+void pf_format_e(double x, int w, int d, char* out);
+/* One summary.dat record, format (i6, 8e15.7) (src/var_diff.f90:1070-1071,
+ * :1161): step, f_int, f_ch, f_eta, e_tot, c_max, c_min, phi_min, phi_P_max.
+ * out holds at least 128 bytes; no newline. */
+void pf_format_summary(int step, const pf_diag* d, char* out);
+/* gfortran list-directed output of one INTEGER*4 (width 12) or REAL*8
+ * (width 25, 17 significant digits), as in time_step.dat and
+ * gamma_matrix.dat; out holds at least 32 bytes. */
+void pf_format_list_int(int v, char* out);
+void pf_format_list_real(double v, char* out);
+
 /* Seeded starts (host only).  Draw order z, y, x (x fastest), per cell var phi
  * values then c, U(-a, a) = a (2 r - 1), r from ran_2 with idum = -(seed+1).
  * pf_ic_voronoi first draws n_grains points (Nx r, Ny r, Nz r); every cell

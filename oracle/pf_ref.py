@@ -319,12 +319,13 @@ def _ellipsoid_offsets(rx: int, ry: int, rz: int):
 
 
 def ic_circle(p: Params, grn_rad: int, ppt_rad, num_ppt: int, iseed: int,
-              c_mat: float, con_0_ppt: float):
+              c_mat: float, con_0_ppt: float, gen: Optional["Ran2"] = None):
     """'circle' start, ``src/var_diff.f90:373-449`` (one rank: ist=1, ien=N).
 
     phi_1 = 1 everywhere, a spherical grain of variant 2 at the centre, then
     num_ppt precipitates (variant 3, c = con_0_ppt) placed at ran_2 positions
     that are rejected while any cell of the sphere already has phi_var > 0.
+    ``gen`` carries ran_2's saved state on to a later precipitate insertion.
     Returns (phi, con, idum_after)."""
     var = p.var
     phi = np.zeros((var,) + p.shape)
@@ -336,7 +337,7 @@ def ic_circle(p: Params, grn_rad: int, ppt_rad, num_ppt: int, iseed: int,
             phi[1, kk - 1, jj - 1, ii - 1] = 1.0
             phi[0, kk - 1, jj - 1, ii - 1] = 0.0
             phi[2, kk - 1, jj - 1, ii - 1] = 0.0
-    gen = Ran2()
+    gen = Ran2() if gen is None else gen
     idum = iseed
     rad_ppt = ppt_rad[0] ** 2 + ppt_rad[1] ** 2 + ppt_rad[2] ** 2
     zz, yy, xx = np.meshgrid(np.arange(1, p.Nz + 1), np.arange(1, p.Ny + 1),
@@ -384,6 +385,42 @@ def ic_plane(p: Params, ppt_rad, i_ppt: int, j_ppt: int, k_ppt: int, c_mat: floa
                 phi[0, kk - 1, jj_ - 1, ii - 1] = 0.0
                 phi[1, kk - 1, jj_ - 1, ii - 1] = 0.0
     return phi, con
+
+
+def insert_precipitates(p: Params, phi: np.ndarray, ppt_rad, num_ppt: int, idum: int, gen: "Ran2"):
+    """Precipitates added at step ``ppt_int``, ``src/var_diff.f90:479-554``
+    (one rank).  A ran_2 position is rejected while the matrix variants there
+    have sum phi_i^2 > 0.8 (inside a grain) or any cell of the sphere already
+    has phi_var > 0; an accepted sphere gets phi_var = 1 and the matrix
+    variants 0 (con is left as it is).  Modifies phi in place; returns
+    idum_after."""
+    var = p.var
+    rad_ppt = ppt_rad[0] ** 2 + ppt_rad[1] ** 2 + ppt_rad[2] ** 2
+    zz, yy, xx = np.meshgrid(np.arange(1, p.Nz + 1), np.arange(1, p.Ny + 1),
+                             np.arange(1, p.Nx + 1), indexing="ij")
+    nppt = 1
+    while nppt <= num_ppt:
+        r, idum = gen(idum)
+        ix = int(r * p.Nx + 1.0)
+        r, idum = gen(idum)
+        jy = int(r * p.Ny + 1.0)
+        r, idum = gen(idum)
+        kz = int(r * p.Nz + 1.0)
+        s = 0.0
+        if 1 <= ix <= p.Nx and 1 <= jy <= p.Ny and 1 <= kz <= p.Nz:
+            for f in range(var - 1):
+                s += float(phi[f, kz - 1, jy - 1, ix - 1]) ** 2
+        if s > 0.8:
+            continue
+        rad = (xx - ix) ** 2 + (yy - jy) ** 2 + (zz - kz) ** 2
+        inside = rad <= rad_ppt
+        if np.any(inside & (phi[var - 1] > 0.0)):
+            continue
+        phi[var - 1][inside] = 1.0
+        for f in range(var - 1):
+            phi[f][inside] = 0.0
+        nppt += 1
+    return idum
 
 
 # ---------------------------------------------------------------------------

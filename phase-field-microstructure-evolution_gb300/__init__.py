@@ -10,7 +10,11 @@ missing.
 from . import build as build_mod
 from .pfgpu import (Batch, Config, Diag, PFError, Ran2, Run, load_library, library_path, make_config,
                     ic_noise, ic_voronoi, ic_noise_aos, ic_voronoi_aos, to_aos, from_aos,
-                    PF_FP32_FUSED, PF_FP64_PLAIN, PF_MOB_C1MC, PF_MOB_REFERENCE, EXPORTED)
+                    PF_FP32_FUSED, PF_FP64_PLAIN, PF_MOB_C1MC, PF_MOB_REFERENCE, EXPORTED,
+                    PF_OK, PF_EINVAL, PF_ECUDA, PF_ENOMEM, PF_ENONFINITE, PF_EIO,
+                    Input, read_input, input_to_config, write_data_save, read_data_save, ic_circle, ic_plane,
+                    ic_polycryst, insert_precipitates, format_e, format_summary, format_list_int,
+                    format_list_real, driver_path)
 
 
 def build(force: bool = False, verbose: bool = False):

@@ -18,6 +18,8 @@ CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 INCLUDE = HERE.parent / "include"
 LIB = OUT / "libpfgpu.so"
+DRIVER = HERE / "driver" / "pf_var_diff.cpp"
+EXE = OUT / "pf_var_diff"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
@@ -82,7 +84,27 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"linking libpfgpu.so failed:\n{r.stdout}\n{r.stderr}")
+    build_driver(nvcc, force, verbose)
     return LIB
+
+
+def build_driver(nvcc: Path, force: bool = False, verbose: bool = False) -> Path:
+    """Link the ``pf_var_diff`` executable (the var_diff.x drop-in) against the library."""
+    if not force and EXE.exists() and EXE.stat().st_mtime >= max(
+            DRIVER.stat().st_mtime, LIB.stat().st_mtime, *(p.stat().st_mtime for p in INCLUDE.glob("*.h"))):
+        return EXE
+    cxx = shutil.which("g++") or str(nvcc)
+    cmd = [cxx, "-O2", "-std=c++17", "-I", str(INCLUDE), str(DRIVER), "-o", str(EXE),
+           "-L", str(OUT), "-lpfgpu", "-Wl,-rpath,$ORIGIN"]
+    if cxx == str(nvcc):
+        cmd = [cxx, "-O2", "-std=c++17", "-I", str(INCLUDE), str(DRIVER), "-o", str(EXE),
+               "-L", str(OUT), "-lpfgpu", "-Xlinker", "-rpath=$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"linking pf_var_diff failed:\n{r.stdout}\n{r.stderr}")
+    return EXE
 
 
 if __name__ == "__main__":

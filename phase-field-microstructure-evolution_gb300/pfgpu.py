@@ -23,7 +23,10 @@ EXPORTED = (
     "pf_create", "pf_supported_shape", "pf_set_fields", "pf_step", "pf_get_fields", "pf_destroy",
     "pf_last_error", "pf_batch_create", "pf_batch_set_fields", "pf_batch_step", "pf_batch_get_fields",
     "pf_batch_destroy", "f_trans_", "inv_trans_", "k_space_", "pf_shim_device", "pf_ran2_init", "pf_ran2",
-    "pf_ic_noise", "pf_ic_voronoi",
+    "pf_ic_noise", "pf_ic_voronoi", "pf_diag_fields_noalloc", "pf_io_last_error", "pf_read_input",
+    "pf_input_to_config", "pf_write_data_save", "pf_read_data_save", "pf_ic_circle", "pf_ic_plane",
+    "pf_ic_polycryst", "pf_insert_precipitates", "pf_format_e", "pf_format_summary", "pf_format_list_int",
+    "pf_format_list_real",
 )
 
 
@@ -59,6 +62,29 @@ class Diag(C.Structure):
 class Ran2State(C.Structure):
     _fields_ = [("idum2", C.c_int), ("iy", C.c_int), ("iv", C.c_int * 32), ("initialised", C.c_int),
                 ("pad", C.c_int * 5)]
+
+
+class Input(C.Structure):
+    """pf_input: the values of input.txt plus the key=value extensions."""
+    _fields_ = [
+        ("nrun", C.c_int), ("ppt_int", C.c_int), ("ppt_rad", C.c_int * 3), ("N_step", C.c_int),
+        ("ifreq", C.c_int), ("i_ppt", C.c_int), ("j_ppt", C.c_int), ("k_ppt", C.c_int), ("iseed", C.c_int),
+        ("grn_rad", C.c_int), ("num_ppt", C.c_int), ("c_mat", C.c_double), ("c_ppt", C.c_double),
+        ("Nx", C.c_int), ("Ny", C.c_int), ("Nz", C.c_int), ("var", C.c_int),
+        ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("t_step", C.c_double),
+        ("grad_coeff_phi", C.c_double), ("grad_coeff_c", C.c_double), ("D_S", C.c_double),
+        ("D_L", C.c_double), ("D_gb", C.c_double), ("mob_phi", C.c_double),
+        ("sigma_1", C.c_double), ("sigma_2", C.c_double),
+        ("am", C.c_double), ("ap", C.c_double), ("con_0_mat", C.c_double), ("con_0_ppt", C.c_double),
+        ("gb_force", C.c_double), ("ndim", C.c_int), ("dims", C.c_int * 2), ("start", C.c_char * 16),
+        ("set_mask", C.c_ulonglong),
+        ("seed", C.c_int), ("n_grains", C.c_int), ("mobility_code", C.c_int), ("precision", C.c_int),
+        ("amp_phi", C.c_double), ("amp_c", C.c_double), ("c0", C.c_double), ("microstructure", C.c_char * 256),
+    ]
+
+    @property
+    def mobility(self):
+        return "c1mc" if self.mobility_code == PF_MOB_C1MC else "reference"
 
 
 _LIB = None
@@ -108,6 +134,21 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_ran2": (C.c_double, [P(Ran2State), ip]),
         "pf_ic_noise": (C.c_int, [P(Config), C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]),
         "pf_ic_voronoi": (C.c_int, [P(Config), C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]),
+        "pf_diag_fields_noalloc": (C.c_int, [P(Config), C.c_void_p, P(Diag), C.c_void_p]),
+        "pf_io_last_error": (C.c_char_p, []),
+        "pf_read_input": (C.c_int, [C.c_char_p, C.c_int, P(Input)]),
+        "pf_input_to_config": (None, [P(Input), P(Config)]),
+        "pf_write_data_save": (C.c_int, [C.c_char_p, P(Config), dp, dp]),
+        "pf_read_data_save": (C.c_int, [C.c_char_p, P(Config), dp, dp]),
+        "pf_ic_circle": (C.c_int, [P(Config), C.c_int, ip, C.c_int, ip, C.c_double, C.c_double, P(Ran2State),
+                                   dp, dp]),
+        "pf_ic_plane": (C.c_int, [P(Config), ip, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]),
+        "pf_ic_polycryst": (C.c_int, [P(Config), C.c_char_p, C.c_double, dp, dp]),
+        "pf_insert_precipitates": (C.c_int, [P(Config), ip, C.c_int, ip, P(Ran2State), dp]),
+        "pf_format_e": (None, [C.c_double, C.c_int, C.c_int, C.c_char_p]),
+        "pf_format_summary": (None, [C.c_int, P(Diag), C.c_char_p]),
+        "pf_format_list_int": (None, [C.c_int, C.c_char_p]),
+        "pf_format_list_real": (None, [C.c_double, C.c_char_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -294,3 +335,114 @@ class Ran2:
 
     def next(self) -> float:
         return self.lib.pf_ran2(C.byref(self.st), C.byref(self.idum))
+
+
+# ---------------------------------------------------------------------------
+# input.txt, restart files, the reference's starts and output formats
+# ---------------------------------------------------------------------------
+def _check_io(rc: int):
+    if rc != PF_OK:
+        raise PFError(rc, load_library().pf_io_last_error().decode())
+
+
+def driver_path() -> Path:
+    """The pf_var_diff executable (built next to the library)."""
+    return _build.EXE
+
+
+def read_input(path, nprocs: int = 1) -> Input:
+    """input.txt with Fortran list-directed rules (pf_read_input)."""
+    lib = load_library()
+    rec = Input()
+    _check_io(lib.pf_read_input(str(path).encode(), nprocs, C.byref(rec)))
+    return rec
+
+
+def input_to_config(rec: Input) -> Config:
+    c = Config()
+    load_library().pf_input_to_config(C.byref(rec), C.byref(c))
+    return c
+
+
+def write_data_save(path, p, phi: np.ndarray, con: np.ndarray):
+    """data_save file of phi[ivar,z,y,x], con[z,y,x] (REAL*8, Fortran unformatted)."""
+    lib = load_library()
+    cfg = make_config(p)
+    a = to_aos(phi)
+    c = np.ascontiguousarray(con, dtype=np.float64)
+    _check_io(lib.pf_write_data_save(str(path).encode(), C.byref(cfg), _dp(a), _dp(c)))
+
+
+def read_data_save(path, p):
+    lib = load_library()
+    cfg = make_config(p)
+    a = np.empty((p.Nz, p.Ny, p.Nx, p.var))
+    c = np.empty((p.Nz, p.Ny, p.Nx))
+    _check_io(lib.pf_read_data_save(str(path).encode(), C.byref(cfg), _dp(a), _dp(c)))
+    return from_aos(a), c
+
+
+def _ints(v):
+    return (C.c_int * len(v))(*[int(x) for x in v])
+
+
+def ic_circle(p, grn_rad: int, ppt_rad, num_ppt: int, iseed: int, c_mat: float, con_0_ppt: float,
+              rng: Optional["Ran2"] = None):
+    """'circle' start; returns (phi, con, rng) with rng advanced (its idum too)."""
+    lib = load_library()
+    rng = rng or Ran2(iseed)
+    cfg = make_config(p)
+    a, c = _ic_buffers(p, False)
+    _check_io(lib.pf_ic_circle(C.byref(cfg), grn_rad, _ints(ppt_rad), num_ppt, C.byref(rng.idum), c_mat,
+                               con_0_ppt, C.byref(rng.st), _dp(a), _dp(c)))
+    return from_aos(a), c, rng
+
+
+def ic_plane(p, ppt_rad, i_ppt: int, j_ppt: int, k_ppt: int, c_mat: float):
+    lib = load_library()
+    cfg = make_config(p)
+    a, c = _ic_buffers(p, False)
+    _check_io(lib.pf_ic_plane(C.byref(cfg), _ints(ppt_rad), i_ppt, j_ppt, k_ppt, c_mat, _dp(a), _dp(c)))
+    return from_aos(a), c
+
+
+def ic_polycryst(p, path, c_mat: float):
+    lib = load_library()
+    cfg = make_config(p)
+    a, c = _ic_buffers(p, False)
+    _check_io(lib.pf_ic_polycryst(C.byref(cfg), str(path).encode(), c_mat, _dp(a), _dp(c)))
+    return from_aos(a), c
+
+
+def insert_precipitates(p, phi: np.ndarray, ppt_rad, num_ppt: int, rng: "Ran2") -> np.ndarray:
+    """Precipitate insertion of step ppt_int; returns the new phi (rng advanced)."""
+    lib = load_library()
+    cfg = make_config(p)
+    a = to_aos(phi)
+    _check_io(lib.pf_insert_precipitates(C.byref(cfg), _ints(ppt_rad), num_ppt, C.byref(rng.idum),
+                                         C.byref(rng.st), _dp(a)))
+    return from_aos(a)
+
+
+def format_e(x: float, w: int, d: int) -> str:
+    buf = C.create_string_buffer(w + 8)
+    load_library().pf_format_e(x, w, d, buf)
+    return buf.value.decode()
+
+
+def format_summary(step: int, diag: Diag) -> str:
+    buf = C.create_string_buffer(256)
+    load_library().pf_format_summary(step, C.byref(diag), buf)
+    return buf.value.decode()
+
+
+def format_list_int(v: int) -> str:
+    buf = C.create_string_buffer(64)
+    load_library().pf_format_list_int(v, buf)
+    return buf.value.decode()
+
+
+def format_list_real(v: float) -> str:
+    buf = C.create_string_buffer(64)
+    load_library().pf_format_list_real(v, buf)
+    return buf.value.decode()

@@ -1,0 +1,326 @@
+"""Host side of the drop-in driver: the input.txt reader (Fortran
+list-directed rules), data_save / data_rerun files, the reference's starts
+and precipitate insertion (against the oracle, bit for bit) and the output
+formats of time_step.dat, gamma_matrix.dat and summary.dat.  No GPU."""
+import os
+import struct
+import subprocess
+
+import numpy as np
+import pytest
+
+HEADER_TIME_STEP = "# step number, iteration duration," + " " * 31 + "run time elapsed"
+HEADER_SUMMARY = ("# step number, f_int_tot, f_ch_tot," + " " * 9 +
+                  "f_eta_tot, e_tot, c_max_glob, c_min_glob, phi_min_glob, phi_3_max")
+HEADER_TIMING = ("# step number, " + ", ".join(f"loop {i} avg" for i in range(1, 8)) + "," + " " * 40 +
+                 ", ".join(f"loop {i} avg" for i in range(8, 15)) + "," + " " * 40 +
+                 "loop duration, run time elapsed")
+
+
+def canonical_input(path, **kw):
+    """input.txt in the layout tests/run_phase_sim.py:112-128 writes."""
+    q = dict(ppt_int=4, N_step=10, ifreq=5, num_ppt=3, c_mat=0.3, c_ppt=0.7, Nx=32, Ny=32, Nz=32, var=3,
+             t_step=0.002, grad_coeff_phi=1.0, grad_coeff_c=1.0, D_S=1.0, D_L=1.0, d_gb=0.5, mob_phi=1.0,
+             sigma_1=1.5, sigma_2=1.5, am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7, gb_force=0.0,
+             dims=(1, 2), start="circle", grn_rad=8, ppt_rad=(2, 2, 2), ijk_ppt=(16, 20, 16), iseed=-1,
+             extra="")
+    q.update(kw)
+    r = q["ppt_rad"]
+    i, j, k = q["ijk_ppt"]
+    with open(path, "w") as f:
+        f.write(f"1 {q['ppt_int']}       / nrun, ppt_int \n")
+        f.write(f"{r[0]} {r[1]} {r[2]} {q['N_step']} {q['ifreq']}      / ppt_rad(3), N_step, ifreq\n")
+        f.write(f"{i} {j} {k} {q['iseed']}        / i_ppt, j_ppt, k_ppt, iseed\n")
+        f.write(f"{q['grn_rad']} {q['num_ppt']} {q['c_mat']} {q['c_ppt']} / grn_rad, num_ppt, c_mat, c_ppt \n")
+        f.write(f"{q['Nx']} {q['Ny']} {q['Nz']} {q['var']} 0.001 0.001 0.001 {q['t_step']}  "
+                "/ Nx, Ny, Nz, var, dx, dy, dz, t_step\n")
+        f.write(f"{q['grad_coeff_phi']} {q['grad_coeff_c']} {q['D_S']} {q['D_L']} {q['d_gb']} {q['mob_phi']}   "
+                "/ grad_coeff_phi, grad_coeff_c, D_S, D_L, d_gb, mob_phi\n")
+        f.write(f"{q['sigma_1']}  {q['sigma_2']}  / sigma_1, sigma_2\n")
+        f.write(f"{q['am']} {q['ap']} {q['con_0_mat']} {q['con_0_ppt']} {q['gb_force']}     "
+                "/ am, ap, con_0_mat, con_0_ppt, gb_force\n")
+        f.write("2       / ndim\n")
+        f.write(f"{q['dims'][0]} {q['dims'][1]}     / dims(2)\n")
+        f.write(f"'{q['start']}'         / start\n")
+        f.write(q["extra"])
+    return path
+
+
+def test_read_canonical(pkg, tmp_path):
+    rec = pkg.read_input(canonical_input(tmp_path / "input.txt"))
+    assert (rec.nrun, rec.ppt_int, list(rec.ppt_rad), rec.N_step, rec.ifreq) == (1, 4, [2, 2, 2], 10, 5)
+    assert (rec.i_ppt, rec.j_ppt, rec.k_ppt, rec.iseed) == (16, 20, 16, -1)
+    assert (rec.grn_rad, rec.num_ppt, rec.c_mat, rec.c_ppt) == (8, 3, 0.3, 0.7)
+    assert (rec.Nx, rec.Ny, rec.Nz, rec.var, rec.dx, rec.t_step) == (32, 32, 32, 3, 0.001, 0.002)
+    assert (rec.grad_coeff_phi, rec.grad_coeff_c, rec.D_S, rec.D_L, rec.D_gb, rec.mob_phi) == \
+        (1.0, 1.0, 1.0, 1.0, 0.5, 1.0)
+    assert (rec.sigma_1, rec.sigma_2, rec.am, rec.ap, rec.con_0_mat, rec.con_0_ppt, rec.gb_force) == \
+        (1.5, 1.5, 0.5, 2.0, 0.3, 0.7, 0.0)
+    assert (rec.ndim, list(rec.dims), rec.start) == (2, [1, 2], b"circle")
+    assert rec.set_mask == (1 << 28) - 1
+    assert rec.precision == 0 and rec.mobility == "reference"
+
+
+def test_read_short_records(pkg, tmp_path):
+    """A '/' before all items of a READ are read leaves the rest untouched; the
+    next READ starts on the next line (an input laid out for an older list of
+    variables is read with the values shifted, as var_diff.x reads it)."""
+    p = tmp_path / "input.txt"
+    p.write_text("1       / nrun\n"
+                 "4 4 4 50000 1000      / ppt_rad(3), N_step, ifreq\n"
+                 "48 70 48 -1        / i_ppt, j_ppt, k_ppt, iseed\n"
+                 "40 50  / grn_rad, num_ppt\n"
+                 "96 96 96 3 0.01 0.01 0.01 1.e-4  / Nx, Ny, Nz, var, dx, dy, dz, t_step\n"
+                 "1.0 1.0 1.0 10.0 5.0   / grad_coeff_phi, grad_coeff_c, d_bulk, d_gb, mob_phi\n"
+                 "6.0  3.0  / sigma_1, sigma_2\n"
+                 "0.5 2.0 0.3 0.7 0.0     / am, ap, con_0_mat, con_0_ppt, gb_force\n"
+                 "1       / ndim\n"
+                 "'circle'         / start\n"
+                 "0.6919  1.02  / sigma_1, sigma_2\n")
+    rec = pkg.read_input(p, nprocs=4)
+    assert rec.nrun == 1 and not rec.set_mask & (1 << 1)           # ppt_int not read
+    assert (rec.N_step, rec.ifreq, rec.grn_rad, rec.num_ppt) == (50000, 1000, 40, 50)
+    assert not rec.set_mask & (1 << 9) and not rec.set_mask & (1 << 10)  # c_mat, c_ppt not read
+    assert (rec.D_S, rec.D_L, rec.D_gb) == (1.0, 10.0, 5.0) and not rec.set_mask & (1 << 20)
+    assert (rec.t_step, rec.sigma_1, rec.sigma_2) == (1e-4, 6.0, 3.0)
+    assert (rec.ndim, list(rec.dims), rec.start) == (1, [1, 4], b"circle")
+
+
+def test_list_directed_syntax(pkg, tmp_path):
+    p = tmp_path / "input.txt"
+    p.write_text("2,7\n"
+                 "3*2\n"
+                 "  100 10\n"
+                 "\n"
+                 "1 2 3 -5\n"
+                 "4 1 0.25d0 7.5D-1\n"
+                 "16 16\n 32 2\n 1.0 1.0 1.0, 1.5e-3\n"
+                 "2*1.0 1.0 2.0 0.0 1.0\n"
+                 "1.5 2.5\n"
+                 "0.5 2.0 0.3 0.7 0.0\n"
+                 "1\n"
+                 "'it''s'\n"
+                 "seed=5 n_grains=12 mobility=c1mc\n"
+                 "precision=64 microstructure=grains.txt amp_phi=0.2 c0=0.4\n")
+    rec = pkg.read_input(p)
+    assert (rec.nrun, rec.ppt_int, list(rec.ppt_rad), rec.N_step, rec.ifreq) == (2, 7, [2, 2, 2], 100, 10)
+    assert (rec.c_mat, rec.c_ppt) == (0.25, 0.75)
+    assert (rec.Nx, rec.Ny, rec.Nz, rec.var, rec.t_step) == (16, 16, 32, 2, 1.5e-3)
+    assert (rec.grad_coeff_phi, rec.grad_coeff_c, rec.D_L, rec.D_gb, rec.mob_phi) == (1.0, 1.0, 2.0, 0.0, 1.0)
+    assert rec.start == b"it's"
+    assert (rec.seed, rec.n_grains, rec.mobility, rec.precision) == (5, 12, "c1mc", 64)
+    assert rec.microstructure == b"grains.txt" and (rec.amp_phi, rec.c0) == (0.2, 0.4)
+    cfg = pkg.input_to_config(rec)
+    assert (cfg.nx, cfg.nz, cfg.var, cfg.mobility, cfg.precision, cfg.sigma_2) == (16, 32, 2, 1, 64, 2.5)
+
+
+def test_read_errors(pkg, tmp_path):
+    with pytest.raises(pkg.PFError) as e:
+        pkg.read_input(tmp_path / "missing.txt")
+    assert e.value.code == pkg.PF_EIO
+    p = tmp_path / "short.txt"
+    p.write_text("1 1\n2 2 2 10 5\n")
+    with pytest.raises(pkg.PFError) as e:
+        pkg.read_input(p)
+    assert e.value.code == pkg.PF_EINVAL
+
+
+def _fields(oracle, p, seed=3):
+    rng = np.random.default_rng(seed)
+    return rng.random((p.var,) + p.shape), rng.random(p.shape)
+
+
+def test_data_save_layout_and_roundtrip(pkg, oracle, tmp_path):
+    p = oracle.Params(Nx=8, Ny=6, Nz=4, var=3)
+    phi, con = _fields(oracle, p)
+    path = tmp_path / "data_save.0001"
+    pkg.write_data_save(path, p, phi, con)
+    raw = path.read_bytes()
+    n = 8 * 6 * 4
+    assert struct.unpack("<i6ii", raw[:32]) == (24, 1, 1, 1, 8, 6, 4, 24)
+    body = n * (p.var + 1) * 8
+    assert len(raw) == 32 + 4 + body + 4
+    assert struct.unpack("<i", raw[32:36])[0] == body and struct.unpack("<i", raw[-4:])[0] == body
+    vals = np.frombuffer(raw[36:36 + body], dtype="<f8")
+    assert np.array_equal(vals[:n * p.var], oracle.to_fortran_aos(phi))
+    assert np.array_equal(vals[n * p.var:], con.reshape(-1))
+    phi2, con2 = pkg.read_data_save(path, p)
+    assert np.array_equal(phi2, phi) and np.array_equal(con2, con)
+
+
+def test_data_rerun_subrecords(pkg, oracle, tmp_path):
+    """A record split into gfortran sub-records (negative continuation markers)
+    reads like one record."""
+    p = oracle.Params(Nx=4, Ny=4, Nz=4, var=2)
+    phi, con = _fields(oracle, p, seed=9)
+    payload = np.concatenate([oracle.to_fortran_aos(phi), con.reshape(-1)]).astype("<f8").tobytes()
+    cuts = [0, 200, 904, len(payload)]
+    out = struct.pack("<i6ii", 24, 1, 1, 1, 4, 4, 4, 24)
+    for s in range(3):
+        part = payload[cuts[s]:cuts[s + 1]]
+        head = len(part) if s == 2 else -len(part)
+        tail = len(part) if s == 0 else -len(part)
+        out += struct.pack("<i", head) + part + struct.pack("<i", tail)
+    path = tmp_path / "data_rerun.0001"
+    path.write_bytes(out)
+    phi2, con2 = pkg.read_data_save(path, p)
+    assert np.array_equal(phi2, phi) and np.array_equal(con2, con)
+
+
+def test_data_save_rejects_other_grid(pkg, oracle, tmp_path):
+    p = oracle.Params(Nx=4, Ny=4, Nz=4, var=2)
+    phi, con = _fields(oracle, p)
+    path = tmp_path / "d"
+    pkg.write_data_save(path, p, phi, con)
+    with pytest.raises(pkg.PFError) as e:
+        pkg.read_data_save(path, oracle.Params(Nx=8, Ny=4, Nz=2, var=2))
+    assert e.value.code == pkg.PF_EIO
+
+
+def _fortran_e(x, w, d):
+    """Ew.d written out in Python (0.ddddE+ee, 3-digit exponents drop the E)."""
+    if x == 0:
+        s = ("-" if np.signbit(x) else "") + "0." + "0" * d + "E+00"
+    else:
+        m, e = f"{abs(x):.{d - 1}e}".split("e")
+        e = int(e) + 1
+        digits = m.replace(".", "")
+        ex = f"E{'-' if e < 0 else '+'}{abs(e):02d}" if abs(e) < 100 else f"{'-' if e < 0 else '+'}{abs(e):03d}"
+        s = ("-" if x < 0 else "") + "0." + digits + ex
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+def test_format_e(pkg):
+    assert pkg.format_e(1.0, 15, 7) == "  0.1000000E+01"
+    assert pkg.format_e(-2.5e-3, 15, 7) == " -0.2500000E-02"
+    assert pkg.format_e(0.0, 15, 7) == "  0.0000000E+00"
+    assert pkg.format_e(9.99999999, 15, 7) == "  0.1000000E+02"
+    assert pkg.format_e(1.5e-120, 15, 7) == "  0.1500000-119"
+    rng = np.random.default_rng(0)
+    for x in np.concatenate([rng.standard_normal(200) * 10.0 ** rng.integers(-30, 30, 200), [1e300, -1e-300]]):
+        assert pkg.format_e(float(x), 15, 7) == _fortran_e(float(x), 15, 7)
+
+
+def test_format_summary(pkg):
+    d = pkg.Diag()
+    vals = dict(f_int=12.5, f_ch=-3.25e-4, f_eta=-1234.5678, e_tot=12.5 - 3.25e-4 - 1234.5678, c_max=0.9,
+                c_min=0.1, phi_min=0.75, phi_P_max=1.0)
+    for k, v in vals.items():
+        setattr(d, k, v)
+    line = pkg.format_summary(42, d)
+    assert len(line) == 6 + 8 * 15 and line[:6] == "    42"
+    cols = [line[6 + 15 * i: 6 + 15 * (i + 1)] for i in range(8)]
+    order = ["f_int", "f_ch", "f_eta", "e_tot", "c_max", "c_min", "phi_min", "phi_P_max"]
+    for c, k in zip(cols, order):
+        assert c == _fortran_e(vals[k], 15, 7)
+        assert abs(float(c) - vals[k]) <= 5e-7 * abs(vals[k])  # 7 significant digits
+
+
+def test_list_directed_output(pkg):
+    """gfortran list-directed INTEGER*4 and REAL*8 items."""
+    assert pkg.format_list_int(7) == "           7"
+    assert pkg.format_list_int(-123) == "        -123"
+    assert pkg.format_list_real(1.0) == "   1.0000000000000000     "
+    assert pkg.format_list_real(0.5) == "  0.50000000000000000     "
+    assert pkg.format_list_real(-1.0) == "  -1.0000000000000000     "
+    assert pkg.format_list_real(0.0) == "   0.0000000000000000     "
+    assert pkg.format_list_real(1.5e-3) == "   1.5000000000000000E-003"
+    assert pkg.format_list_real(123456.0) == "   123456.00000000000     "
+    assert pkg.format_list_real(1e20) == "   1.0000000000000000E+020"
+    for v in (3.14159, 2.5e-7, 7.0e12, -0.125):
+        s = pkg.format_list_real(v)
+        assert len(s) == 26 and float(s) == v
+
+
+def test_ic_circle_matches_oracle(pkg, oracle):
+    p = oracle.Params(Nx=32, Ny=32, Nz=16, var=3)
+    gen = oracle.Ran2()
+    phi_o, con_o, idum_o = oracle.ic_circle(p, 8, (2, 3, 2), 4, -1, 0.3, 0.7, gen=gen)
+    phi, con, rng = pkg.ic_circle(p, 8, (2, 3, 2), 4, -1, 0.3, 0.7)
+    assert np.array_equal(phi, phi_o) and np.array_equal(con, con_o)
+    assert rng.idum.value == idum_o
+    # the saved state carries on: the next draws agree
+    idum = idum_o
+    for _ in range(5):
+        v, idum = gen(idum)
+        assert rng.next() == v
+    assert np.count_nonzero(phi[2]) > 0 and np.all(con[phi[2] > 0] == 0.7)
+
+
+def test_ic_plane_matches_oracle(pkg, oracle):
+    p = oracle.Params(Nx=16, Ny=32, Nz=16, var=3)
+    phi_o, con_o = oracle.ic_plane(p, (3, 2, 4), 8, 20, 8, 0.25)
+    phi, con = pkg.ic_plane(p, (3, 2, 4), 8, 20, 8, 0.25)
+    assert np.array_equal(phi, phi_o) and np.array_equal(con, con_o)
+
+
+def test_ic_polycryst(pkg, oracle, tmp_path):
+    p = oracle.Params(Nx=8, Ny=4, Nz=4, var=5)
+    rng = np.random.default_rng(4)
+    lab = rng.integers(1, p.var + 1, p.shape)
+    path = tmp_path / "mc_ivar_fin"
+    with open(path, "w") as f:
+        for k in range(1, p.Nz + 1):
+            for j in range(1, p.Ny + 1):
+                for i in range(1, p.Nx + 1):
+                    f.write(f"{i} {j} {k} {lab[k - 1, j - 1, i - 1]}\n")
+    phi, con = pkg.ic_polycryst(p, path, 0.3)
+    want = np.zeros((p.var,) + p.shape)
+    for v in range(p.var):
+        want[v][lab == v + 1] = 1.0
+    assert np.array_equal(phi, want) and np.all(con == 0.3)
+    (tmp_path / "short").write_text("1 1 1 1\n")
+    with pytest.raises(pkg.PFError):
+        pkg.ic_polycryst(p, tmp_path / "short", 0.3)
+
+
+def test_insert_precipitates_matches_oracle(pkg, oracle):
+    p = oracle.Params(Nx=32, Ny=32, Nz=32, var=5)
+    phi0, _ = oracle.ic_voronoi(p, 2, 6, 0.0, 0.5, 0.0)
+    # soften the grain boundaries so that some positions are admissible
+    phi0 = phi0 * 0.6
+    gen = oracle.Ran2()
+    idum = -7
+    phi_o = phi0.copy()
+    idum_o = oracle.insert_precipitates(p, phi_o, (2, 2, 2), 5, idum, gen)
+    rng = pkg.Ran2(-7)
+    phi = pkg.insert_precipitates(p, phi0, (2, 2, 2), 5, rng)
+    assert np.array_equal(phi, phi_o)
+    assert rng.idum.value == idum_o
+    assert np.count_nonzero(phi[-1] == 1.0) >= 5
+
+
+def test_driver_writes_headers(pkg, oracle, tmp_path):
+    """Without a GPU the driver writes its headers and gamma_matrix.dat, then
+    stops at pf_create with status 2; with one it runs to the end."""
+    exe = pkg.driver_path()
+    assert exe.exists()
+    inp = canonical_input(tmp_path / "input.txt", N_step=2, ifreq=2, num_ppt=1)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(exe), str(inp), str(out) + "/"], cwd=tmp_path, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode in (0, 2), r.stderr
+    if r.returncode == 2:
+        assert "pf_create" in r.stderr
+    assert (out / "time_step.dat").read_text().split("\n")[0] == HEADER_TIME_STEP
+    assert (out / "summary.dat").read_text().split("\n")[0] == HEADER_SUMMARY
+    assert (out / "timing_data.dat").read_text().split("\n")[0] == HEADER_TIMING
+    g = oracle.gamma_matrix(3, 1.5, 1.5)
+    lines = (out / "gamma_matrix.dat").read_text().strip("\n").split("\n")
+    assert len(lines) == 3
+    for i, line in enumerate(lines):
+        assert line == pkg.format_list_int(i + 1) + "".join(pkg.format_list_real(float(x)) for x in g[i])
+
+
+def test_driver_usage_and_bad_input(pkg, tmp_path):
+    exe = str(pkg.driver_path())
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "usage" in r.stderr
+    r = subprocess.run([exe, str(tmp_path / "nope.txt")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "cannot open" in r.stderr
+    inp = canonical_input(tmp_path / "input.txt", Nx=20)
+    r = subprocess.run([exe, str(inp), str(tmp_path) + "/"], capture_output=True, text=True, timeout=60)
+    if r.returncode == 2 and "not supported" in r.stderr:
+        return
+    assert r.returncode in (0, 2)
