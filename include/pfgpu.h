@@ -234,6 +234,40 @@ void pf_format_summary(int step, const pf_diag* d, char* out);
 void pf_format_list_int(int v, char* out);
 void pf_format_list_real(double v, char* out);
 
+/* ---- voxel analysis of the post-processor paraview.x (src/paraview.f90) ---
+ * Per voxel (src/paraview.f90:189-244): phi_sq = sum_i phi_i^2; var_num = the
+ * last variant with phi_i > 0.8 (0 if none); phi_3 = phi_3 (index 3 is fixed
+ * in the reference); boundary = 1.0 where more than one phi_i > threshold;
+ * grad_phi_3 = |grad phi_3| by central differences on interior cells, 0 on
+ * the outer layer (:380-429).  Counts: boundary voxels, boundary voxels with
+ * phi_var > threshold, and their ratio (0 without boundary voxels).  FP64 with
+ * the reference's order of operations.  Needs var >= 3. */
+typedef struct pf_voxel_counts {
+  long long precipitate_voxels, boundary_voxels;
+  double precipitate_fraction;
+} pf_voxel_counts;
+/* Host arrays of nx*ny*nz values in con(x,y,z) order; any may be NULL (not
+ * computed / not copied back). */
+typedef struct pf_analysis_out {
+  double* phi_sq;
+  int* var_num;
+  double* phi_3;
+  double* grad_phi_3;
+  double* boundary;
+  double* con; /* pf_analyze_run only: the run's c */
+} pf_analysis_out;
+/* Fields from host arrays (phi(var,x,y,z), con(x,y,z)) on cfg->device. */
+int pf_analyze_fields(const pf_config* cfg, const double* phi_aos, const double* con, double threshold,
+                      const pf_analysis_out* out, pf_voxel_counts* counts);
+/* The resident fields of a run, with no host copy of the fields (out may be
+ * NULL for the counts alone).  Leaves the run's state unchanged. */
+int pf_analyze_run(pf_run* run, double threshold, const pf_analysis_out* out, pf_voxel_counts* counts);
+/* An ASCII VTK file as paraview.f90:277-296 writes it: the fixed
+ * STRUCTURED_POINTS header, then every value as one gfortran list-directed
+ * record (REAL*8 or INTEGER*4 items), formatted on all host cores. */
+int pf_write_vtk_real(const char* path, int nx, int ny, int nz, const double* v);
+int pf_write_vtk_int(const char* path, int nx, int ny, int nz, const int* v);
+
 /* Seeded starts (host only).  Draw order z, y, x (x fastest), per cell var phi
  * values then c, U(-a, a) = a (2 r - 1), r from ran_2 with idum = -(seed+1).
  * pf_ic_voronoi first draws n_grains points (Nx r, Ny r, Nz r); every cell

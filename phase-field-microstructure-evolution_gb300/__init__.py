@@ -14,7 +14,8 @@ from .pfgpu import (Batch, Config, Diag, PFError, Ran2, Run, load_library, libra
                     PF_OK, PF_EINVAL, PF_ECUDA, PF_ENOMEM, PF_ENONFINITE, PF_EIO,
                     Input, read_input, input_to_config, write_data_save, read_data_save, ic_circle, ic_plane,
                     ic_polycryst, insert_precipitates, format_e, format_summary, format_list_int,
-                    format_list_real, driver_path)
+                    format_list_real, driver_path, VoxelCounts, AnalysisOut, analyze_fields, analyze_run,
+                    write_vtk, paraview_path)
 
 
 def build(force: bool = False, verbose: bool = False):

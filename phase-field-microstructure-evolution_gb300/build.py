@@ -18,8 +18,9 @@ CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 INCLUDE = HERE.parent / "include"
 LIB = OUT / "libpfgpu.so"
-DRIVER = HERE / "driver" / "pf_var_diff.cpp"
-EXE = OUT / "pf_var_diff"
+DRIVERS = HERE / "driver"
+EXE = OUT / "pf_var_diff"          # the var_diff.x drop-in
+PARAVIEW_EXE = OUT / "pf_paraview"  # the paraview.x drop-in
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
@@ -88,23 +89,23 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     return LIB
 
 
-def build_driver(nvcc: Path, force: bool = False, verbose: bool = False) -> Path:
-    """Link the ``pf_var_diff`` executable (the var_diff.x drop-in) against the library."""
-    if not force and EXE.exists() and EXE.stat().st_mtime >= max(
-            DRIVER.stat().st_mtime, LIB.stat().st_mtime, *(p.stat().st_mtime for p in INCLUDE.glob("*.h"))):
-        return EXE
+def build_driver(nvcc: Path, force: bool = False, verbose: bool = False):
+    """Link the executables of ``driver/`` (the var_diff.x and paraview.x
+    drop-ins) against the library."""
+    hdr = max(p.stat().st_mtime for p in INCLUDE.glob("*.h"))
     cxx = shutil.which("g++") or str(nvcc)
-    cmd = [cxx, "-O2", "-std=c++17", "-I", str(INCLUDE), str(DRIVER), "-o", str(EXE),
-           "-L", str(OUT), "-lpfgpu", "-Wl,-rpath,$ORIGIN"]
-    if cxx == str(nvcc):
-        cmd = [cxx, "-O2", "-std=c++17", "-I", str(INCLUDE), str(DRIVER), "-o", str(EXE),
-               "-L", str(OUT), "-lpfgpu", "-Xlinker", "-rpath=$ORIGIN"]
-    if verbose:
-        print(" ".join(cmd), flush=True)
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"linking pf_var_diff failed:\n{r.stdout}\n{r.stderr}")
-    return EXE
+    for src in sorted(DRIVERS.glob("*.cpp")):
+        exe = OUT / src.stem
+        if not force and exe.exists() and exe.stat().st_mtime >= max(src.stat().st_mtime, LIB.stat().st_mtime, hdr):
+            continue
+        rpath = ["-Wl,-rpath,$ORIGIN"] if cxx != str(nvcc) else ["-Xlinker", "-rpath=$ORIGIN"]
+        cmd = [cxx, "-O2", "-std=c++17", "-I", str(INCLUDE), str(src), "-o", str(exe),
+               "-L", str(OUT), "-lpfgpu"] + rpath
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"linking {exe.name} failed:\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":

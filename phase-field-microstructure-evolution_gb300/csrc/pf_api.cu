@@ -612,6 +612,23 @@ static int batch_get_fields(pf_batch* b, int run, double* phi, double* con) {
   return PF_OK;
 }
 
+// Real-space fields of run 0 of a batch in the float staging buffer fin.
+static int batch_device_fields(pf_batch* b, DeviceFields* out) {
+  PF_CUDA(cudaSetDevice(b->device));
+  const size_t ncell = (size_t)b->Nx * b->Ny * b->Nz;
+  const dim3 gx(b->Nz * (b->Ny / b->xk.wy), 1);
+  b->xk.exp<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp, b->tab.sh);
+  PF_CUDA(cudaGetLastError());
+  out->phi = b->fin;
+  out->con = b->fin + (size_t)b->V * ncell;
+  out->is_double = 0;
+  out->fstride = ncell;
+  out->cstride = 1;
+  out->nx = b->Nx; out->ny = b->Ny; out->nz = b->Nz; out->var = b->V; out->device = b->device;
+  out->stream = b->stream;
+  return PF_OK;
+}
+
 static void fill_diag(const double* d, pf_diag* o) {
   o->step = (int)d[DR_STEP];
   o->nonfinite = (int)d[DR_NONFINITE];
@@ -658,6 +675,14 @@ static int batch_step(pf_batch* b, int nsteps, pf_diag* diag) {
   if (bad) return fail(PF_ENONFINITE, "a step produced non-finite values");
   return PF_OK;
 }
+
+namespace pf {
+int run_device_fields(pf_run* run, DeviceFields* out) {
+  if (!run || !out) return fail(PF_EINVAL, "null argument");
+  if (run->p64) return plain64_device_fields(run->p64, out);
+  return batch_device_fields(run->b, out);
+}
+}  // namespace pf
 
 // ---------------------------------------------------------------------------
 // exported C ABI

@@ -16,6 +16,7 @@
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/pfgpu.h"
@@ -513,6 +514,61 @@ void pf_format_list_real(double v, char* out) {
                                         }()).c_str());
   }
   snprintf(out, 32, " %s", body);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// ASCII VTK files of paraview.f90:277-296
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T, size_t W, typename F>
+int write_vtk(const char* path, int nx, int ny, int nz, const T* v, F fmt) {
+  if (!path || !v || nx < 1 || ny < 1 || nz < 1) return io_fail(PF_EINVAL, "null argument to the VTK writer");
+  const size_t n = (size_t)nx * ny * nz;
+  FILE* f = fopen(path, "w");
+  if (!f) return io_fail(PF_EIO, std::string("cannot create ") + path);
+  fprintf(f, "# vtk DataFile Version 3.0\nSample Data\nASCII\nDATASET STRUCTURED_POINTS\n");
+  fprintf(f, "DIMENSIONS  %6d%6d%6d\nASPECT_RATIO 1.0 1.0 1.0\nORIGIN 0.0 0.0 0.0\n", nx, ny, nz);
+  fprintf(f, "POINT_DATA  %12lld\nSCALARS Field double 1\nLOOKUP_TABLE default\n", (long long)n);
+  // every item has a fixed width W: format blocks of values on all cores
+  const size_t block = (size_t)1 << 18;
+  const int nth = std::max(1, (int)std::thread::hardware_concurrency());
+  std::vector<char> buf(std::min(n, block * nth) * W + 1);
+  bool ok = true;
+  for (size_t base = 0; base < n && ok; base += block * nth) {
+    const size_t cnt = std::min(n - base, block * nth);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t) {
+      const size_t a = (size_t)t * block, b = std::min(cnt, a + block);
+      if (a >= b) break;
+      th.emplace_back([&, a, b] {
+        char item[40];
+        for (size_t i = a; i < b; ++i) {
+          fmt(v[base + i], item);
+          memcpy(&buf[i * W], item, W);
+        }
+      });
+    }
+    for (auto& t : th) t.join();
+    ok = fwrite(buf.data(), 1, cnt * W, f) == cnt * W;
+  }
+  ok = ok && fputc('\n', f) != EOF;
+  ok = (fclose(f) == 0) && ok;
+  return ok ? PF_OK : io_fail(PF_EIO, std::string("write failed: ") + path);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pf_write_vtk_real(const char* path, int nx, int ny, int nz, const double* v) {
+  return write_vtk<double, 26>(path, nx, ny, nz, v, [](double x, char* out) { pf_format_list_real(x, out); });
+}
+
+int pf_write_vtk_int(const char* path, int nx, int ny, int nz, const int* v) {
+  return write_vtk<int, 12>(path, nx, ny, nz, v, [](int x, char* out) { pf_format_list_int(x, out); });
 }
 
 }  // extern "C"

@@ -389,6 +389,19 @@ int plain64_get_fields(Plain64* p, double* phi, double* con) {
   return PF_OK;
 }
 
+int plain64_device_fields(Plain64* p, DeviceFields* out) {
+  if (!p || !out) return fail64(PF_EINVAL, "bad arguments to device_fields");
+  P64_CUDA(cudaSetDevice(p->device));
+  out->phi = p->phi;
+  out->con = p->con;
+  out->is_double = 1;
+  out->fstride = p->ncell;
+  out->cstride = 1;
+  out->nx = p->Nx; out->ny = p->Ny; out->nz = p->Nz; out->var = p->V; out->device = p->device;
+  out->stream = p->stream;
+  return PF_OK;
+}
+
 static int one_step(Plain64* p, double* acc_out) {
   const size_t n = p->ncell, ns = p->nspec;
   const double scale = 1.0 / (double)n;  // f_trans normalisation (src/f_trans.f90:12)

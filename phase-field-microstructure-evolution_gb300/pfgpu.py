@@ -26,7 +26,7 @@ EXPORTED = (
     "pf_ic_noise", "pf_ic_voronoi", "pf_diag_fields_noalloc", "pf_io_last_error", "pf_read_input",
     "pf_input_to_config", "pf_write_data_save", "pf_read_data_save", "pf_ic_circle", "pf_ic_plane",
     "pf_ic_polycryst", "pf_insert_precipitates", "pf_format_e", "pf_format_summary", "pf_format_list_int",
-    "pf_format_list_real",
+    "pf_format_list_real", "pf_analyze_fields", "pf_analyze_run", "pf_write_vtk_real", "pf_write_vtk_int",
 )
 
 
@@ -85,6 +85,17 @@ class Input(C.Structure):
     @property
     def mobility(self):
         return "c1mc" if self.mobility_code == PF_MOB_C1MC else "reference"
+
+
+class VoxelCounts(C.Structure):
+    _fields_ = [("precipitate_voxels", C.c_longlong), ("boundary_voxels", C.c_longlong),
+                ("precipitate_fraction", C.c_double)]
+
+
+class AnalysisOut(C.Structure):
+    _fields_ = [("phi_sq", C.POINTER(C.c_double)), ("var_num", C.POINTER(C.c_int)),
+                ("phi_3", C.POINTER(C.c_double)), ("grad_phi_3", C.POINTER(C.c_double)),
+                ("boundary", C.POINTER(C.c_double)), ("con", C.POINTER(C.c_double))]
 
 
 _LIB = None
@@ -149,6 +160,10 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_format_summary": (None, [C.c_int, P(Diag), C.c_char_p]),
         "pf_format_list_int": (None, [C.c_int, C.c_char_p]),
         "pf_format_list_real": (None, [C.c_double, C.c_char_p]),
+        "pf_analyze_fields": (C.c_int, [P(Config), dp, dp, C.c_double, P(AnalysisOut), P(VoxelCounts)]),
+        "pf_analyze_run": (C.c_int, [C.c_void_p, C.c_double, P(AnalysisOut), P(VoxelCounts)]),
+        "pf_write_vtk_real": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, dp]),
+        "pf_write_vtk_int": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, P(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -446,3 +461,67 @@ def format_list_real(v: float) -> str:
     buf = C.create_string_buffer(64)
     load_library().pf_format_list_real(v, buf)
     return buf.value.decode()
+
+
+# ---------------------------------------------------------------------------
+# voxel analysis of paraview.x and its VTK files
+# ---------------------------------------------------------------------------
+ANALYSIS_FIELDS = ("phi_sq", "var_num", "phi_3", "grad_phi_3", "boundary", "con")
+
+
+def _analysis_out(shape, want):
+    arrays, out = {}, AnalysisOut()
+    for k in ANALYSIS_FIELDS:
+        if k in want:
+            a = np.empty(shape, dtype=np.int32 if k == "var_num" else np.float64)
+            arrays[k] = a
+            setattr(out, k, a.ctypes.data_as(C.POINTER(C.c_int if k == "var_num" else C.c_double)))
+    return arrays, out
+
+
+def _counts(c: VoxelCounts) -> dict:
+    return dict(precipitate_voxels=c.precipitate_voxels, boundary_voxels=c.boundary_voxels,
+                precipitate_fraction=c.precipitate_fraction)
+
+
+def analyze_fields(p, phi: np.ndarray, con: np.ndarray, threshold: float, device: int = 0,
+                   want=ANALYSIS_FIELDS[:5]) -> dict:
+    """GPU voxel analysis of phi[ivar,z,y,x], con[z,y,x]; arrays are [z,y,x]."""
+    lib = load_library()
+    cfg = make_config(p, device=device)
+    a = to_aos(phi)
+    c = np.ascontiguousarray(con, dtype=np.float64)
+    arrays, out = _analysis_out((p.Nz, p.Ny, p.Nx), [k for k in want if k != "con"])
+    cnt = VoxelCounts()
+    _check(lib.pf_analyze_fields(C.byref(cfg), _dp(a), _dp(c), threshold, C.byref(out), C.byref(cnt)))
+    arrays.update(_counts(cnt))
+    return arrays
+
+
+def analyze_run(run: "Run", threshold: float, want=()) -> dict:
+    """In-situ analysis of a run's resident fields (counts, plus the arrays in want)."""
+    lib = load_library()
+    p = run.p
+    arrays, out = _analysis_out((p.Nz, p.Ny, p.Nx), want)
+    cnt = VoxelCounts()
+    _check(lib.pf_analyze_run(run.h, threshold, C.byref(out) if want else None, C.byref(cnt)))
+    arrays.update(_counts(cnt))
+    return arrays
+
+
+def write_vtk(path, values: np.ndarray):
+    """ASCII VTK file of values[z, y, x] (float64 or int32) in paraview.x's layout."""
+    lib = load_library()
+    nz, ny, nx = values.shape
+    if values.dtype.kind in "iu":
+        v = np.ascontiguousarray(values, dtype=np.int32)
+        rc = lib.pf_write_vtk_int(str(path).encode(), nx, ny, nz, v.ctypes.data_as(C.POINTER(C.c_int)))
+    else:
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        rc = lib.pf_write_vtk_real(str(path).encode(), nx, ny, nz, _dp(v))
+    _check_io(rc)
+
+
+def paraview_path() -> Path:
+    """The pf_paraview executable (built next to the library)."""
+    return _build.PARAVIEW_EXE
