@@ -80,10 +80,12 @@ typedef struct pf_run pf_run;
 /* ---- step-level API (replaces src/var_diff.f90:474-1118) ---------------- */
 
 /* Create a run on cfg->device: validates the sizes, allocates the resident
- * state and builds the FP64 wavenumber/twiddle tables.  Supported grids:
- * Nx, Ny, Nz in {16, 32, 64, 128, 256} (FP32 path; every (Ny, Nz) pair with
- * Ny == Nz plus the non-cubic pairs listed by pf_supported_shape), 1 <= var
- * <= 48. */
+ * state and builds the FP64 wavenumber/twiddle tables.  Supported grids on
+ * the fused FP32 path: Nx, Ny, Nz in {16, 32, 64, 96, 128, 256} (every
+ * (Ny, Nz) pair with Ny == Nz plus the non-cubic pairs listed by
+ * pf_supported_shape), 1 <= var <= 255 as long as var+1 field rows of the x
+ * pass fit in shared memory (var <= 131 at Nx = 96, 98 at 128, 105 at 256).
+ * The FP64 path takes any even Nx. */
 int pf_create(const pf_config* cfg, pf_run** out);
 
 /* 1 if (nx, ny, nz, var) can run on the given precision path, else 0. */

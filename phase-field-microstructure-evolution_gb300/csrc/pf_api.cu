@@ -191,6 +191,7 @@ static size_t x_smem(int nx, int nF, int wy) {
     case 16: pitch = Line<8>::PITCH; break;
     case 32: pitch = Line<16>::PITCH; break;
     case 64: pitch = Line<32>::PITCH; break;
+    case 96: pitch = Line<48>::PITCH; break;
     case 128: pitch = Line<64>::PITCH; break;
     case 256: pitch = Line<128>::PITCH; break;
     default: return 0;
@@ -199,16 +200,19 @@ static size_t x_smem(int nx, int nF, int wy) {
 }
 
 static const size_t kMaxSmem = 227 * 1024;
+// order parameters per run; the x pass must also fit (var+1) field lines of
+// its rows in shared memory (checked below)
+static const int kMaxVar = 255;
 
 static int validate(const pf_config* c) {
   if (!c) return fail(PF_EINVAL, "null config");
   XKernels xv[kMaxVariants];
   YZKernels yk;
   const int nxv = get_x_variants(c->nx, xv);
-  if (nxv == 0) return fail(PF_EINVAL, "Nx=%d not supported (16, 32, 64, 128, 256)", c->nx);
+  if (nxv == 0) return fail(PF_EINVAL, "Nx=%d not supported (16, 32, 64, 96, 128, 256)", c->nx);
   if (!get_yz_kernels(c->ny, c->nz, &yk))
     return fail(PF_EINVAL, "(Ny, Nz)=(%d, %d) not supported by the fused FP32 path", c->ny, c->nz);
-  if (c->var < 1 || c->var > 48) return fail(PF_EINVAL, "var=%d outside [1, 48]", c->var);
+  if (c->var < 1 || c->var > kMaxVar) return fail(PF_EINVAL, "var=%d outside [1, %d]", c->var, kMaxVar);
   bool fits = false;
   for (int i = 0; i < nxv; ++i)
     fits = fits || (c->ny % xv[i].wy == 0 && x_smem(c->nx, c->var + 1, xv[i].wy) <= kMaxSmem);

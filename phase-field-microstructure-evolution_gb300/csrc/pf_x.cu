@@ -23,6 +23,7 @@ int x_variants_a(int nx, XKernels* out, int n) {
     case 16: n = add<16, 16, 256>(out, n); break;
     case 32: n = add<32, 16, 256>(out, n); n = add<32, 8, 128>(out, n); break;
     case 64: n = add<64, 8, 256>(out, n); n = add<64, 16, 256>(out, n); n = add<64, 4, 128>(out, n); break;
+    case 96: n = add<96, 8, 256>(out, n); n = add<96, 4, 256>(out, n); n = add<96, 16, 256>(out, n); break;
     case 128:
       n = add<128, 8, 256>(out, n);
       n = add<128, 4, 256>(out, n);

@@ -47,6 +47,11 @@ int yz_variants_small(int ny, int nz, YZKernels* out, int n) {
     n = add1<64, 64, 512>(out, n);
     n = add<64, 64, 2, 256>(out, n);
   }
+  if (ny == 96 && nz == 96) {  // the reference's own grid (inputs/config.yaml, inputs/input.txt)
+    n = add1<96, 96, 384>(out, n);
+    n = add1<96, 96, 192>(out, n);
+    n = add1<96, 96, 768>(out, n);
+  }
   return n;
 }
 

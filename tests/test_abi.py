@@ -32,15 +32,22 @@ def test_supported_shapes(lib):
     assert lib.pf_supported_shape(128, 128, 128, 16, 32) == 1
     assert lib.pf_supported_shape(256, 256, 256, 32, 32) == 1
     assert lib.pf_supported_shape(64, 32, 64, 4, 32) == 1
-    assert lib.pf_supported_shape(96, 96, 96, 4, 32) == 0  # not a fused-path size
-    assert lib.pf_supported_shape(96, 96, 96, 4, 64) == 1  # the FP64 path takes any even Nx
-    assert lib.pf_supported_shape(128, 128, 128, 64, 32) == 0  # var limit
+    assert lib.pf_supported_shape(96, 96, 96, 55, 32) == 1  # the reference's own grid and var
+    assert lib.pf_supported_shape(48, 48, 48, 4, 32) == 0  # not a fused-path size
+    assert lib.pf_supported_shape(48, 48, 48, 4, 64) == 1  # the FP64 path takes any even Nx
+    assert lib.pf_supported_shape(128, 128, 128, 98, 32) == 1
+    assert lib.pf_supported_shape(128, 128, 128, 99, 32) == 0  # x-pass rows no longer fit
+    assert lib.pf_supported_shape(96, 96, 96, 131, 32) == 1
+    assert lib.pf_supported_shape(96, 96, 96, 132, 32) == 0
+    assert lib.pf_supported_shape(256, 256, 256, 105, 32) == 1
+    assert lib.pf_supported_shape(256, 256, 256, 106, 32) == 0
+    assert lib.pf_supported_shape(64, 64, 64, 256, 32) == 0  # var limit
 
 
 def test_create_rejects_bad_config(pkg, oracle):
     with pytest.raises(pkg.PFError) as e:
-        pkg.Run(oracle.Params(96, 96, 96, 4))
-    assert e.value.code == -1 and "Nx=96" in str(e.value)
+        pkg.Run(oracle.Params(48, 48, 48, 4))
+    assert e.value.code == -1 and "Nx=48" in str(e.value)
 
 
 def test_k_space_shim_matches_oracle(lib, oracle):

@@ -127,6 +127,40 @@ def test_fp32_256cube_cluster(pkg, oracle):
     _check_fields(gp, gc, op, oc, TOL32)
 
 
+def test_fp32_96cube_reference_grid(pkg, oracle):
+    """The reference's own grid (96^3, inputs/config.yaml) with variable mobility."""
+    p = oracle.Params(96, 96, 96, 8, t_step=0.005, D_gb=0.5, am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7)
+    phi, con = oracle.ic_voronoi(p, 8, 12, 0.02, 0.4, 0.02)
+    gp, gc, gd = _run_lib(pkg, p, phi, con, 20)
+    op, oc, od = oracle.run(p, phi, con, 20, faithful=False, workers=8)
+    _check_fields(gp, gc, op, oc, TOL32)
+    _check_diag(gd, od, TOL32, oracle.stats(phi, con))
+
+
+def test_fp32_many_order_parameters(pkg, oracle):
+    """var = 55 (the reference's baseline configuration) on a 32^3 grid."""
+    p = oracle.Params(32, 32, 32, 55, t_step=0.005, D_gb=1.0, am=0.5, ap=5.0, con_0_mat=0.1, con_0_ppt=1.0)
+    phi, con = oracle.ic_voronoi(p, 9, 40, 0.02, 0.5, 0.02)
+    gp, gc, gd = _run_lib(pkg, p, phi, con, 10)
+    op, oc, od = oracle.run(p, phi, con, 10, faithful=False, workers=8)
+    _check_fields(gp, gc, op, oc, TOL32)
+    _check_diag(gd, od, TOL32, oracle.stats(phi, con))
+
+
+def test_fp32_vs_fp64_reference_baseline_config(pkg, oracle):
+    """inputs/config.yaml's baseline (96^3, var = 55, am 0.5, ap 5, c0 0.1/1,
+    D_gb 1, dt 1e-4) on both GPU paths: the fused FP32 path against the FP64
+    cuFFT path over 20 steps."""
+    p = oracle.Params(96, 96, 96, 55, t_step=1e-4, D_gb=1.0, am=0.5, ap=5.0, con_0_mat=0.1, con_0_ppt=1.0)
+    phi, con = oracle.ic_voronoi(p, 11, 64, 0.02, 0.5, 0.02)
+    gp, gc, gd = _run_lib(pkg, p, phi, con, 20)
+    hp, hc, hd = _run_lib(pkg, p, phi, con, 20, precision=64)
+    _check_fields(gp, gc, hp, hc, TOL32)
+    for a, b in zip(gd, hd):
+        for k in ("f_int", "f_eta", "f_ch", "c_min", "c_max", "phi_min", "phi_P_max"):
+            assert abs(a[k] - b[k]) <= TOL32 * max(1.0, abs(b[k])), (a["step"], k, a[k], b[k])
+
+
 @pytest.mark.parametrize("mob", ["reference", "c1mc"])
 def test_fp64_plain_vs_oracle(pkg, oracle, mob):
     p = oracle.Params(16, 16, 16, 3, t_step=0.01, D_gb=1.0, am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7,
