@@ -46,7 +46,8 @@ enum Mobility { MOB_CONST = 0, MOB_REF_VAR = 1, MOB_C1MC = 2 };
 
 // Device-side description of one run (all runs of a launch share one shape)
 struct RunParams {
-  float2* Sk;      // [nF][Kx][Ny][Nz] state in k-space (digit-transposed y, z positions)
+  float2* Sk;      // [nF][Kx] planes of the k-space state (digit-transposed y, z positions; the
+                   // order inside a plane belongs to the yz-pass variant that runs the batch)
   float2* Sm;      // [nF][Kx][Nz][Ny] state in mixed space (x spectrum, real-space y, z)
   float2* D;       // [nF][Kx][Nz][Ny] x-spectra of dF/dphi_i and dF/dc
   float* mob;      // [Nz][Ny][Nx] mobility minus D_mean (variable mobility only)
@@ -1030,15 +1031,14 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
       const int ky = LY::freq_of_pos(yp);
       const float qy2 = __ldg(sh.qy2 + ky), qy4 = __ldg(sh.qy4 + ky), qn_y = __ldg(sh.qny + ky);
       float2* pc = U + (k2 * N1z) * PY + LY::phys(yp);
-      float2* gk = rp.Sk + poff + (size_t)yp * NZ + k2 * N1z;  // k-space state run
+      // k-space state of this plane in [k1][k2][y position] order: for every
+      // k1 a warp reads and writes 32 consecutive y positions (coalesced)
+      float2* gk = rp.Sk + poff + (size_t)k2 * NY + yp;
+      constexpr size_t SK1 = (size_t)N2z * NY;  // stride of k1
       float2 d[N1z], u[N1z];
       if (MODE != YZ_IMPORT) {
 #pragma unroll
-        for (int k1 = 0; k1 < N1z; k1 += 2) {
-          const float4 t = *reinterpret_cast<const float4*>(gk + k1);
-          u[k1] = make_float2(t.x, t.y);
-          u[k1 + 1] = make_float2(t.z, t.w);
-        }
+        for (int k1 = 0; k1 < N1z; ++k1) u[k1] = gk[k1 * SK1];
       }
 #pragma unroll
       for (int k1 = 0; k1 < N1z; ++k1) d[k1] = pc[k1 * PY];
@@ -1089,8 +1089,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
         }
       }
 #pragma unroll
-      for (int k1 = 0; k1 < N1z; k1 += 2)
-        *reinterpret_cast<float4*>(gk + k1) = make_float4(u[k1].x, u[k1].y, u[k1 + 1].x, u[k1 + 1].y);
+      for (int k1 = 0; k1 < N1z; ++k1) gk[k1 * SK1] = u[k1];
       if (MODE != YZ_IMPORT) {
         if (var_c) {
           dft_inv<N1z>(d);
