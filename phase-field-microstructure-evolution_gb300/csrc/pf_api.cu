@@ -778,6 +778,14 @@ int pf_batch_enqueue(pf_batch* b, int nsteps) {
 void* pf_batch_stream(pf_batch* b) { return b ? (void*)b->stream : nullptr; }
 const char* pf_batch_variant(pf_batch* b) { return b ? b->variant.c_str() : ""; }
 pf_batch* pf_run_batch(pf_run* r) { return r ? r->b : nullptr; }
+// Number of compiled x-pass and yz-pass variants of a grid (the index range
+// of PFGPU_X_VARIANT / PFGPU_YZ_VARIANT).
+void pf_variant_counts(int nx, int ny, int nz, int* nxv, int* nyzv) {
+  XKernels xv[kMaxVariants];
+  YZKernels yv[kMaxVariants];
+  if (nxv) *nxv = get_x_variants(nx, xv);
+  if (nyzv) *nyzv = get_yz_variants(ny, nz, yv);
+}
 // Launch the x pass / yz pass alone (kernel timing); returns PF_OK.
 int pf_batch_enqueue_phase(pf_batch* b, int phase) {
   if (!b) return fail(PF_EINVAL, "null batch");

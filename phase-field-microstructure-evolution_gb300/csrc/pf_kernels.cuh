@@ -499,9 +499,10 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
   if (MODE != MODE_BULK) return;
 
   // 6. diagnostics: block reduction into per-block partials
-  __shared__ double red_d[3][8];
-  __shared__ float red_f[4][8];
-  __shared__ int red_i[8];
+  static_assert(T % 32 == 0 && T <= 1024, "whole warps");
+  __shared__ double red_d[3][T / 32];  // one slot per warp
+  __shared__ float red_f[4][T / 32];
+  __shared__ int red_i[T / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double s0 = warp_sum((double)acc.feta), s1 = warp_sum((double)acc.fch), s2 = warp_sum((double)acc.mass);
   float m0 = warp_min(acc.cmin), m1 = warp_max(acc.cmax), m2 = warp_min(acc.phimin), m3 = warp_max(acc.phipmax);
@@ -787,18 +788,17 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
       const int ky = LY::freq_of_pos(ypos);
       const float qy2 = __ldg(sh.qy2 + ky), qy4 = __ldg(sh.qy4 + ky), qn_y = __ldg(sh.qny + ky);
       float2* pb = UB + yl * G::PZ + k2 * (N1z + 1);
-      float2* gk = rp.Sk + poff + (size_t)ypos * NZ + k2 * N1z;  // k-space state run
+      // k-space state of this plane in [k1][y position][k2] order: for every
+      // k1 a warp reads and writes consecutive (y position, k2) (coalesced)
+      float2* gk = rp.Sk + poff + (size_t)ypos * N2z + k2;
+      constexpr size_t SK1 = (size_t)NY * N2z;  // stride of k1
       float2 d[N1z], u[N1z];
 #pragma unroll
       for (int k1 = 0; k1 < N1z; ++k1) d[k1] = pb[k1];
       Dft<N1z>::fwd(d);
       if (MODE != YZ_IMPORT) {
 #pragma unroll
-        for (int k1 = 0; k1 < N1z; k1 += 2) {
-          const float4 t = *reinterpret_cast<const float4*>(gk + k1);
-          u[k1] = make_float2(t.x, t.y);
-          u[k1 + 1] = make_float2(t.z, t.w);
-        }
+        for (int k1 = 0; k1 < N1z; ++k1) u[k1] = gk[k1 * SK1];
       }
 #pragma unroll
       for (int k1 = 0; k1 < N1z; ++k1) {
@@ -850,8 +850,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
         }
       }
 #pragma unroll
-      for (int k1 = 0; k1 < N1z; k1 += 2)
-        *reinterpret_cast<float4*>(gk + k1) = make_float4(u[k1].x, u[k1].y, u[k1 + 1].x, u[k1 + 1].y);
+      for (int k1 = 0; k1 < N1z; ++k1) gk[k1 * SK1] = u[k1];
       if (MODE != YZ_IMPORT) {
         if (var_c) {
           dft_inv<N1z>(d);
