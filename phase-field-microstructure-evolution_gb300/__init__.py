@@ -15,7 +15,7 @@ from .pfgpu import (Batch, Config, Diag, PFError, Ran2, Run, load_library, libra
                     Input, read_input, input_to_config, write_data_save, read_data_save, ic_circle, ic_plane,
                     ic_polycryst, insert_precipitates, format_e, format_summary, format_list_int,
                     format_list_real, driver_path, VoxelCounts, AnalysisOut, analyze_fields, analyze_run,
-                    write_vtk, paraview_path)
+                    write_vtk, paraview_path, sweep, sweep_path, variant_counts)
 
 
 def build(force: bool = False, verbose: bool = False):

@@ -21,6 +21,7 @@ LIB = OUT / "libpfgpu.so"
 DRIVERS = HERE / "driver"
 EXE = OUT / "pf_var_diff"          # the var_diff.x drop-in
 PARAVIEW_EXE = OUT / "pf_paraview"  # the paraview.x drop-in
+SWEEP_EXE = OUT / "pf_sweep"        # many var_diff.x cases in one process
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
@@ -92,7 +93,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 def build_driver(nvcc: Path, force: bool = False, verbose: bool = False):
     """Link the executables of ``driver/`` (the var_diff.x and paraview.x
     drop-ins) against the library."""
-    hdr = max(p.stat().st_mtime for p in INCLUDE.glob("*.h"))
+    hdr = max(p.stat().st_mtime for p in list(INCLUDE.glob("*.h")) + list(DRIVERS.glob("*.h")))
     cxx = shutil.which("g++") or str(nvcc)
     for src in sorted(DRIVERS.glob("*.cpp")):
         exe = OUT / src.stem

@@ -137,6 +137,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_batch_stream": (C.c_void_p, [C.c_void_p]),
         "pf_batch_variant": (C.c_char_p, [C.c_void_p]),
         "pf_run_batch": (C.c_void_p, [C.c_void_p]),
+        "pf_variant_counts": (None, [C.c_int, C.c_int, C.c_int, ip, ip]),
         "f_trans_": (None, [dp, dp, ip, ip, ip, ip, ip, ip, ip]),
         "inv_trans_": (None, [dp, dp, ip, ip, ip, ip]),
         "k_space_": (None, [ip, ip, ip, ip, ip, dp, dp, dp]),
@@ -525,3 +526,26 @@ def write_vtk(path, values: np.ndarray):
 def paraview_path() -> Path:
     """The pf_paraview executable (built next to the library)."""
     return _build.PARAVIEW_EXE
+
+
+def sweep_path() -> Path:
+    """The pf_sweep executable (built next to the library)."""
+    return _build.SWEEP_EXE
+
+
+def sweep(case_dirs, max_batch: int = 64, timeout: Optional[float] = None):
+    """Run var_diff.x cases (directories holding an input.txt) through
+    pf_sweep; returns the CompletedProcess (exit status 0 when every case
+    finished, 2 or 3 when one failed; see pf_sweep.cpp)."""
+    import subprocess
+
+    cmd = [str(sweep_path()), "--max-batch", str(max_batch)] + [str(d) for d in case_dirs]
+    return subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
+
+
+def variant_counts(nx: int, ny: int, nz: int):
+    """(x-pass, yz-pass) compiled variants of a grid: the ranges of
+    PFGPU_X_VARIANT and PFGPU_YZ_VARIANT."""
+    a, b = C.c_int(0), C.c_int(0)
+    load_library().pf_variant_counts(nx, ny, nz, C.byref(a), C.byref(b))
+    return a.value, b.value

@@ -324,3 +324,29 @@ def test_driver_usage_and_bad_input(pkg, tmp_path):
     if r.returncode == 2 and "not supported" in r.stderr:
         return
     assert r.returncode in (0, 2)
+
+
+def test_sweep_tool_without_gpu(pkg, oracle, tmp_path):
+    """pf_sweep sets every case up (headers, gamma_matrix.dat, mrun.out), then
+    stops at the GPU with status 2 when there is none; a case without input
+    is reported and the others go on."""
+    exe = str(pkg.sweep_path())
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "usage" in r.stderr
+    dirs = []
+    for i, var in enumerate((3, 3, 4)):
+        d = tmp_path / f"run_{i}"
+        d.mkdir()
+        canonical_input(d / "input.txt", var=var, N_step=2, ifreq=2, ppt_int=0)
+        dirs.append(d)
+    empty = tmp_path / "run_empty"
+    empty.mkdir()
+    r = pkg.sweep(dirs + [empty], timeout=600)
+    assert r.returncode in (0, 2), r.stderr
+    assert "run_empty" in r.stderr and "cannot open" in r.stderr
+    for d in dirs:
+        assert (d / "summary.dat").read_text().split("\n")[0] == HEADER_SUMMARY
+        assert "precipitates assigned" in (d / "mrun.out").read_text()
+    g = oracle.gamma_matrix(4, 1.5, 1.5)
+    lines = (dirs[2] / "gamma_matrix.dat").read_text().strip("\n").split("\n")
+    assert lines[3] == pkg.format_list_int(4) + "".join(pkg.format_list_real(float(x)) for x in g[3])
