@@ -252,6 +252,8 @@ struct pf_batch {
   int ring = 0;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  cudaStream_t side = nullptr;        // second branch of the captured step (diagnostics reduction)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<double> hdiag;
   std::vector<int> steps_done;
   std::string variant;  // chosen kernel variants, for reports
@@ -282,20 +284,36 @@ static int launch_yz(pf_batch* b, KernelFn fn, int planes, const RunParams* runs
   return PF_OK;
 }
 
-static int enqueue_step(pf_batch* b, cudaStream_t s) {
+// One step on stream s.  With `branch` (the captured graph), the diagnostics
+// reduction, which needs only the x pass's and the main yz pass's partials,
+// runs on a second branch beside the concentration chain (xj pass, yz C2
+// pass) under variable mobility, and the step ends when both are done.
+static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
   const Shape sh = b->tab.sh;
   const int R = b->nruns;
   const dim3 gx(b->Nz * (b->Ny / b->xk.wy), R);
   b->xk.bulk<<<gx, b->xk.threads, b->smem_x, s>>>(b->drp, sh);
   int rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, R, s);
   if (rc) return rc;
+  const bool fork = branch && b->mob != MOB_CONST && b->side;
+  if (fork) {
+    PF_CUDA(cudaEventRecord(b->ev_fork, s));
+    PF_CUDA(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
+    reduce_diag_kernel<<<R, 1024, 0, b->side>>>(b->drp, sh);
+    PF_CUDA(cudaGetLastError());
+    PF_CUDA(cudaEventRecord(b->ev_join, b->side));
+  }
   if (b->mob != MOB_CONST) {
     b->xk.xj<<<gx, b->xk.threads, b->smem_xj, s>>>(b->drp, sh);
     rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, s);
     if (rc) return rc;
   }
-  reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
-  PF_CUDA(cudaGetLastError());
+  if (fork) {
+    PF_CUDA(cudaStreamWaitEvent(s, b->ev_join, 0));
+  } else {
+    reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
+    PF_CUDA(cudaGetLastError());
+  }
   return PF_OK;
 }
 
@@ -457,6 +475,9 @@ static void destroy_batch(pf_batch* b) {
   cudaSetDevice(b->device);
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   if (b->stream) cudaStreamDestroy(b->stream);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
   cudaFree(b->drp);
   cudaFree(b->mem);
   cudaFree(b->fin);
@@ -561,6 +582,10 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "run table copy: %s", cudaGetErrorString(e)));
   e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream: %s", cudaGetErrorString(e)));
+  e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream/events: %s", cudaGetErrorString(e)));
 
   rc = tune_batch(b);
   if (rc) return bail(rc);
@@ -569,7 +594,7 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   cudaGraph_t g = nullptr;
   e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "begin capture: %s", cudaGetErrorString(e)));
-  rc = enqueue_step(b, b->stream);
+  rc = enqueue_step(b, b->stream, env_int("PFGPU_REDUCE_BRANCH", 1) != 0);
   cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
   if (rc) { if (g) cudaGraphDestroy(g); return bail(rc); }
   if (e2 != cudaSuccess) return bail(fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2)));
