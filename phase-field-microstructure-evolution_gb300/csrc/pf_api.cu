@@ -12,6 +12,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/pfgpu.h"
@@ -242,6 +243,7 @@ struct pf_batch {
   int mob = MOB_CONST;
   DevTables tab;
   XKernels xk{};
+  XKernels xjk{};              // variant of the xj pass (one field: its best rows per CTA differ)
   YZKernels yk{};
   size_t smem_x = 0, smem_xj = 0;
   std::vector<RunParams> hrp;
@@ -304,7 +306,8 @@ static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
     PF_CUDA(cudaEventRecord(b->ev_join, b->side));
   }
   if (b->mob != MOB_CONST) {
-    b->xk.xj<<<gx, b->xk.threads, b->smem_xj, s>>>(b->drp, sh);
+    const dim3 gj(b->Nz * (b->Ny / b->xjk.wy), R);
+    b->xjk.xj<<<gj, b->xjk.threads, b->smem_xj, s>>>(b->drp, sh);
     rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, s);
     if (rc) return rc;
   }
@@ -332,7 +335,7 @@ __global__ void fill_kernel(float* p, size_t n, float v0, float v1) {
 }
 
 static std::mutex g_tune_mu;
-static std::map<std::string, std::pair<int, int>> g_tune_cache;
+static std::map<std::string, std::tuple<int, int, int>> g_tune_cache;  // x, yz, xj variant
 
 static bool yz_ok(pf_batch* b, const YZKernels& k) {
   if (k.smem > kMaxSmem) return false;
@@ -370,16 +373,34 @@ static bool x_ok(pf_batch* b, const XKernels& k) {
   return true;
 }
 
+// the xj pass works on one field: a variant whose bulk pass does not fit can serve it
+static bool xj_ok(pf_batch* b, const XKernels& k) {
+  if (b->Ny % k.wy != 0) return false;
+  const size_t sm = x_smem(b->Nx, 1, k.wy);
+  return sm <= kMaxSmem &&
+         cudaFuncSetAttribute((const void*)k.xj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess;
+}
+
+static void describe_variants(pf_batch* b) {
+  char buf[160];
+  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d yz:cluster=%d,threads=%d xj:wy=%d,threads=%d", b->xk.wy,
+           b->xk.threads, b->yk.cluster, b->yk.threads, b->xjk.wy, b->xjk.threads);
+  b->variant = buf;
+}
+
+static void apply_xj(pf_batch* b, const XKernels& k) {
+  b->xjk = k;
+  b->smem_xj = x_smem(b->Nx, 1, k.wy);
+  describe_variants(b);
+}
+
 static void apply_variants(pf_batch* b, const XKernels& xk, const YZKernels& yk) {
   b->xk = xk;
   b->yk = yk;
   b->smem_x = x_smem(b->Nx, b->nF, xk.wy);
-  b->smem_xj = x_smem(b->Nx, 1, xk.wy);
   b->tab.sh.nblk_x = b->Nz * (b->Ny / xk.wy);
   b->tab.sh.nblk_yz = yk.cluster * b->nF * b->Kx;
-  char buf[128];
-  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d yz:cluster=%d,threads=%d", xk.wy, xk.threads, yk.cluster, yk.threads);
-  b->variant = buf;
+  apply_xj(b, xk);
 }
 
 static int env_int(const char* name, int dflt) {
@@ -402,14 +423,15 @@ static int tune_batch(pf_batch* b) {
   int dev = 0;
   cudaGetDevice(&dev);
   snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d", b->Nx, b->Ny, b->Nz, b->V, b->mob, dev);
-  int bx = xs[0], by = ys[0];
+  int bx = xs[0], by = ys[0], bj = -1;
   const int fx = env_int("PFGPU_X_VARIANT", -1), fy = env_int("PFGPU_YZ_VARIANT", -1);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-      bx = it->second.first;
-      by = it->second.second;
+      bx = std::get<0>(it->second);
+      by = std::get<1>(it->second);
+      bj = std::get<2>(it->second);
     } else if (env_int("PFGPU_AUTOTUNE", 1) != 0 && (xs.size() > 1 || ys.size() > 1)) {
       // synthetic non-zero state so that the bulk terms take their usual branches
       const size_t nfin = (size_t)b->nF * b->Nx * b->Ny * b->Nz;
@@ -449,6 +471,30 @@ static int tune_batch(pf_batch* b) {
         }
       for (int i : ys)
         if (ty[i] < ty[by]) by = i;
+      // the xj pass (variable mobility) alone, over every variant that fits one field
+      apply_variants(b, xv[bx], yv[by]);
+      bj = bx;
+      if (b->mob != MOB_CONST) {
+        std::vector<float> tj(nx, 1e30f);
+        const int R = b->nruns;
+        for (int round = 0; round < ROUNDS; ++round)
+          for (int i = 0; i < nx; ++i) {
+            if (!xj_ok(b, xv[i])) continue;
+            apply_xj(b, xv[i]);
+            const dim3 gj(b->Nz * (b->Ny / b->xjk.wy), R);
+            b->xjk.xj<<<gj, b->xjk.threads, b->smem_xj, b->stream>>>(b->drp, b->tab.sh);
+            cudaEventRecord(e0, b->stream);
+            for (int r = 0; r < 4 * REPS; ++r)
+              b->xjk.xj<<<gj, b->xjk.threads, b->smem_xj, b->stream>>>(b->drp, b->tab.sh);
+            cudaEventRecord(e1, b->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (cudaGetLastError() == cudaSuccess) tj[i] = std::min(tj[i], ms);
+          }
+        for (int i = 0; i < nx; ++i)
+          if (tj[i] < tj[bj]) bj = i;
+      }
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       PF_CUDA(cudaStreamSynchronize(b->stream));
@@ -461,12 +507,18 @@ static int tune_batch(pf_batch* b) {
         PF_CUDA(cudaMemsetAsync(r.counter, 0, sizeof(int), b->stream));
       }
       PF_CUDA(cudaStreamSynchronize(b->stream));
-      g_tune_cache[key] = std::make_pair(bx, by);
+      g_tune_cache[key] = std::make_tuple(bx, by, bj);
     }
   }
   if (fx >= 0 && fx < nx && x_ok(b, xv[fx])) bx = fx;
   if (fy >= 0 && fy < ny && yz_ok(b, yv[fy])) by = fy;
+  // PFGPU_X_VARIANT forces the xj pass too, unless PFGPU_XJ_VARIANT names its own
+  const int fj = env_int("PFGPU_XJ_VARIANT", -1);
+  if (bj < 0 || (fx >= 0 && fx < nx)) bj = bx;
+  if (fj >= 0 && fj < nx && xj_ok(b, xv[fj])) bj = fj;
+  if (!xj_ok(b, xv[bj])) bj = bx;
   apply_variants(b, xv[bx], yv[by]);
+  apply_xj(b, xv[bj]);
   return PF_OK;
 }
 
