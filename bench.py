@@ -311,7 +311,9 @@ def run_ours(args):
     diag_bytes = 80  # sizeof(pf_diag)
     assert len(recs) == args.steps
 
-    kernels_per_step = 5 if var_mob else 3
+    # x pass, yz pass (order-parameter planes and c planes as two launches on
+    # the graph's two branches), xj pass, yz C2 pass, reduction
+    kernels_per_step = 6 if var_mob else 3
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "cell-steps/s x P", "n_gpus": ws, "steps": args.steps,

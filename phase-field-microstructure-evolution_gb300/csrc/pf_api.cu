@@ -176,6 +176,7 @@ static int build_tables(int Nx, int Ny, int Nz, DevTables& t) {
   char* b = (char*)t.base;
   Shape& s = t.sh;
   s.Nx = Nx; s.Ny = Ny; s.Nz = Nz; s.Kx = Kx;
+  s.plane0 = 0;
   s.twM = (const float2*)(b + off_tw[0]);
   s.twN = (const float2*)(b + off_tw[1]);
   s.twY = (const float2*)(b + off_tw[2]);
@@ -255,7 +256,8 @@ struct pf_batch {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t side = nullptr;        // second branch of the captured step (diagnostics reduction)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_c = nullptr;
+  int prio_hi = 0;                    // greatest stream priority of the device
   std::vector<double> hdiag;
   std::vector<int> steps_done;
   std::string variant;  // chosen kernel variants, for reports
@@ -267,59 +269,92 @@ struct pf_run {
   pf::Plain64* p64 = nullptr;
 };
 
-// One cluster launch of a yz-pass kernel over `planes` (field, kx) planes of
-// `nruns` runs starting at `runs`.
-static int launch_yz(pf_batch* b, KernelFn fn, int planes, const RunParams* runs, int nruns, cudaStream_t s) {
+// One cluster launch of a yz-pass kernel over `planes` (field, kx) planes,
+// from plane `plane0` on, of `nruns` runs starting at `runs`; `prio` != 0
+// gives the launch that scheduling priority.
+static int launch_yz(pf_batch* b, KernelFn fn, int planes, const RunParams* runs, int nruns, cudaStream_t s,
+                     int plane0 = 0, int prio = 0) {
   cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = b->yk.cluster;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributePriority;
+  at[1].val.priority = prio;
   cfg.gridDim = dim3(b->yk.cluster * planes, nruns);
   cfg.blockDim = dim3(b->yk.threads);
   cfg.dynamicSmemBytes = b->yk.smem;
   cfg.stream = s;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
-  PF_CUDA(cudaLaunchKernelEx(&cfg, fn, runs, b->tab.sh));
+  cfg.numAttrs = prio ? 2 : 1;
+  Shape sh = b->tab.sh;
+  sh.plane0 = plane0;
+  PF_CUDA(cudaLaunchKernelEx(&cfg, fn, runs, sh));
   return PF_OK;
 }
 
-// One step on stream s.  With `branch` (the captured graph), the diagnostics
-// reduction, which needs only the x pass's and the main yz pass's partials,
-// runs on a second branch beside the concentration chain (xj pass, yz C2
-// pass) under variable mobility, and the step ends when both are done.
+// The xj pass with an optional scheduling priority.
+static int launch_xj(pf_batch* b, cudaStream_t s, int prio = 0) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = prio;
+  cfg.gridDim = dim3(b->Nz * (b->Ny / b->xjk.wy), b->nruns);
+  cfg.blockDim = dim3(b->xjk.threads);
+  cfg.dynamicSmemBytes = b->smem_xj;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = prio ? 1 : 0;
+  PF_CUDA(cudaLaunchKernelEx(&cfg, b->xjk.xj, (const RunParams*)b->drp, b->tab.sh));
+  return PF_OK;
+}
+
+// One step on stream s.  With `branch` (the captured graph) and variable
+// mobility, the concentration field's chain — its yz planes, the xj pass and
+// the yz C2 pass, which the order-parameter planes do not need — runs on a
+// second branch at high priority beside the order-parameter planes, so that
+// its small launches fill SMs as the big launch drains; the diagnostics
+// reduction follows the order-parameter planes once the c planes' f_int
+// partials are in.
 static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
   const Shape sh = b->tab.sh;
   const int R = b->nruns;
   const dim3 gx(b->Nz * (b->Ny / b->xk.wy), R);
   b->xk.bulk<<<gx, b->xk.threads, b->smem_x, s>>>(b->drp, sh);
-  int rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, R, s);
-  if (rc) return rc;
-  const bool fork = branch && b->mob != MOB_CONST && b->side;
-  if (fork) {
+  const bool var = b->mob != MOB_CONST;
+  if (branch && var && b->side) {
+    const int pc = b->V * b->Kx;  // first plane of the c field
     PF_CUDA(cudaEventRecord(b->ev_fork, s));
     PF_CUDA(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
-    reduce_diag_kernel<<<R, 1024, 0, b->side>>>(b->drp, sh);
-    PF_CUDA(cudaGetLastError());
+    int rc = launch_yz(b, b->yk.main, b->Kx, b->drp, R, b->side, pc, b->prio_hi);
+    if (rc) return rc;
+    PF_CUDA(cudaEventRecord(b->ev_c, b->side));
+    rc = launch_xj(b, b->side, b->prio_hi);
+    if (rc) return rc;
+    rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, b->side, 0, b->prio_hi);
+    if (rc) return rc;
     PF_CUDA(cudaEventRecord(b->ev_join, b->side));
+    rc = launch_yz(b, b->yk.main, pc, b->drp, R, s);
+    if (rc) return rc;
+    PF_CUDA(cudaStreamWaitEvent(s, b->ev_c, 0));
+    reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
+    PF_CUDA(cudaGetLastError());
+    PF_CUDA(cudaStreamWaitEvent(s, b->ev_join, 0));
+    return PF_OK;
   }
-  if (b->mob != MOB_CONST) {
-    const dim3 gj(b->Nz * (b->Ny / b->xjk.wy), R);
-    b->xjk.xj<<<gj, b->xjk.threads, b->smem_xj, s>>>(b->drp, sh);
+  int rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, R, s);
+  if (rc) return rc;
+  if (var) {
+    rc = launch_xj(b, s);
+    if (rc) return rc;
     rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, s);
     if (rc) return rc;
   }
-  if (fork) {
-    PF_CUDA(cudaStreamWaitEvent(s, b->ev_join, 0));
-  } else {
-    reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
-    PF_CUDA(cudaGetLastError());
-  }
+  reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
+  PF_CUDA(cudaGetLastError());
   return PF_OK;
 }
-
 
 // ---------------------------------------------------------------------------
 // Autotuner: time every compiled variant of the x and yz passes on this batch
@@ -530,6 +565,7 @@ static void destroy_batch(pf_batch* b) {
   if (b->side) cudaStreamDestroy(b->side);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->ev_c) cudaEventDestroy(b->ev_c);
   cudaFree(b->drp);
   cudaFree(b->mem);
   cudaFree(b->fin);
@@ -634,7 +670,10 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "run table copy: %s", cudaGetErrorString(e)));
   e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream: %s", cudaGetErrorString(e)));
-  e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+  int prio_lo = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &b->prio_hi);
+  e = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, b->prio_hi);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_c, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream/events: %s", cudaGetErrorString(e)));
@@ -650,7 +689,7 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
   if (rc) { if (g) cudaGraphDestroy(g); return bail(rc); }
   if (e2 != cudaSuccess) return bail(fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2)));
-  e = cudaGraphInstantiate(&b->gexec, g, 0);
+  e = cudaGraphInstantiate(&b->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)));
   *out = b;

@@ -76,6 +76,7 @@ struct Shape {
   const float* qnx; const float* qny; const float* qnz;  // Nyquist-zeroed q_d (kf / i)
   int nblk_x;   // blocks of the x pass per run
   int nblk_yz;  // blocks of the yz pass per run
+  int plane0;   // first (field, kx) plane of a yz-pass launch (a launch may cover a subset)
 };
 
 // ---------------------------------------------------------------------------
@@ -726,7 +727,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   float2* UB = smem + G::UA;
   const RunParams& rp = runs[blockIdx.y];
   const int r = (C == 1) ? 0 : (int)(blockIdx.x % C);
-  const int p = blockIdx.x / C;
+  const int p = sh.plane0 + (int)(blockIdx.x / C);
   const int Kx = sh.Kx;
   const int f = (MODE == YZ_C2) ? rp.V : p / Kx;
   const int kx = p - (p / Kx) * Kx;
@@ -919,7 +920,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
       for (int w = 0; w < T / 32; ++w) s += red[w];
       const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
       const double n3 = (double)sh.Nx * NY * NZ;
-      rp.part_yz[blockIdx.x] = s * wkx * 0.5 * kap * n3;
+      rp.part_yz[(size_t)sh.plane0 * C + blockIdx.x] = s * wkx * 0.5 * kap * n3;
     }
   }
 }
@@ -976,7 +977,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   extern __shared__ float2 U[];
   __shared__ double red[T / 32];
   const RunParams& rp = runs[blockIdx.y];
-  const int p = blockIdx.x;
+  const int p = sh.plane0 + (int)blockIdx.x;
   const int Kx = sh.Kx;
   const int f = (MODE == YZ_C2) ? rp.V : p / Kx;
   const int kx = p - (p / Kx) * Kx;
@@ -1150,7 +1151,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
       for (int q = 0; q < T / 32; ++q) s += red[q];
       const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
       const double n3 = (double)sh.Nx * NY * NZ;
-      rp.part_yz[blockIdx.x] = s * wkx * 0.5 * kap * n3;
+      rp.part_yz[p] = s * wkx * 0.5 * kap * n3;
     }
   }
 }
