@@ -33,6 +33,7 @@ extern "C" {
 #define PF_ENOMEM (-3)     /* device allocation failed */
 #define PF_ENONFINITE (-4) /* a step produced NaN/Inf (fields left as computed) */
 #define PF_EIO (-5)        /* file I/O error */
+#define PF_EBUSY (-6)      /* a wait ran out of time (the work goes on) */
 
 /* mobility forms of the concentration equation */
 #define PF_MOB_REFERENCE 0 /* mob = D_L + 2(1 - sum phi_i^2) D_gb  (src/var_diff.f90:893-898) */
@@ -117,6 +118,50 @@ int pf_batch_set_fields(pf_batch* b, int run, const double* phi_aos, const doubl
 int pf_batch_step(pf_batch* b, int nsteps, pf_diag* diag);
 int pf_batch_get_fields(pf_batch* b, int run, double* phi_aos, double* con);
 int pf_batch_destroy(pf_batch* b);
+
+/* ---- serving: continuous batching of independent runs on one GPU --------
+ * The reference runs a parameter study as one SLURM job per run
+ * (tests/run_phase_sim.py:130-172); a pf_server takes the runs as requests in
+ * one process.  A worker thread admits queued requests as the resident runs
+ * leave room in the device-memory budget and in max_active; waiting requests
+ * of the same grid, var and mobility class are admitted together as one
+ * batch, every batch steps on its own stream, and batches of different shapes
+ * overlap on the device.  A run leaves as soon as its own step count is
+ * reached.  Results do not depend on what else is running (per-run
+ * reductions, no shared state).  Fused FP32 path only. */
+typedef struct pf_server pf_server;
+typedef struct pf_server_config {
+  int device;
+  int max_active;          /* runs resident at once (0: 64) */
+  double hbm_budget_bytes; /* device memory the server's runs may hold (0: 80 % of free memory at create) */
+  int chunk_steps;         /* steps a batch is given at a time (0: 64, at most 1024) */
+  int reserved[5];
+} pf_server_config;
+typedef struct pf_request_times {
+  double queued_s; /* submit -> admitted */
+  double run_s;    /* admitted -> finished */
+  double total_s;  /* submit -> finished */
+} pf_request_times;
+#define PF_REQ_QUEUED 0
+#define PF_REQ_RUNNING 1
+#define PF_REQ_DONE 2
+#define PF_REQ_FAILED 3
+int pf_server_create(const pf_server_config* cfg, pf_server** out);
+/* Queue a run of nsteps steps from the given fields (copied; layout of
+ * pf_set_fields).  *id identifies the request. */
+int pf_server_submit(pf_server* s, const pf_config* cfg, const double* phi_aos, const double* con, int nsteps,
+                     long long* id);
+/* State of a request (PF_REQ_*). */
+int pf_server_poll(pf_server* s, long long id, int* state);
+/* Wait for a request (timeout_s < 0: no limit; PF_EBUSY when it runs out),
+ * then copy its final fields (may be NULL), the record of its last step and
+ * its times, and forget it.  A failed request returns its error code. */
+int pf_server_wait(pf_server* s, long long id, double timeout_s, double* phi_aos, double* con, pf_diag* last,
+                   pf_request_times* times);
+/* Finish the work in flight, fail what is still queued, release everything. */
+int pf_server_destroy(pf_server* s);
+/* Message of the last failed pf_server_* call of the calling thread. */
+const char* pf_server_last_error(void);
 
 /* ---- Fortran compatibility shims (single rank, FP64, whole grid) ---------
  * Same argument lists as the reference subroutines, all by reference, with

@@ -15,7 +15,8 @@ from .pfgpu import (Batch, Config, Diag, PFError, Ran2, Run, load_library, libra
                     Input, read_input, input_to_config, write_data_save, read_data_save, ic_circle, ic_plane,
                     ic_polycryst, insert_precipitates, format_e, format_summary, format_list_int,
                     format_list_real, driver_path, VoxelCounts, AnalysisOut, analyze_fields, analyze_run,
-                    write_vtk, paraview_path, sweep, sweep_path, variant_counts)
+                    write_vtk, paraview_path, sweep, sweep_path, variant_counts, Server, ServerConfig,
+                    RequestTimes, PF_EBUSY, PF_REQ_QUEUED, PF_REQ_RUNNING, PF_REQ_DONE, PF_REQ_FAILED)
 
 
 def build(force: bool = False, verbose: bool = False):

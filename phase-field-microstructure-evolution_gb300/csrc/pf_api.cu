@@ -894,6 +894,39 @@ int pf_batch_enqueue(pf_batch* b, int nsteps) {
 void* pf_batch_stream(pf_batch* b) { return b ? (void*)b->stream : nullptr; }
 const char* pf_batch_variant(pf_batch* b) { return b ? b->variant.c_str() : ""; }
 pf_batch* pf_run_batch(pf_run* r) { return r ? r->b : nullptr; }
+// Device bytes a batch of `nruns` runs of configuration `cfg` holds (the
+// buffers create_batch allocates, rounded up); for admission by HBM budget.
+size_t pf_batch_bytes(const pf_config* c, int nruns) {
+  if (!c || nruns < 1) return 0;
+  const size_t Kx = c->nx / 2 + 1, nF = c->var + 1;
+  const size_t plane = (size_t)c->ny * c->nz, fieldc = Kx * plane, ncell = (size_t)c->nx * plane;
+  const bool var = c->mobility == PF_MOB_C1MC || c->D_gb != 0.0;
+  auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const size_t per_run = 3 * align(nF * fieldc * 8) + (var ? align(ncell * 4) + align(fieldc * 8) : 0) +
+                         align((size_t)XD_COUNT * plane * 8) + align(16 * nF * Kx * 8) + align(1024 * DR_COUNT * 8) + 256;
+  return per_run * nruns + nF * ncell * 12 + ((size_t)1 << 20);
+}
+// Steps run `run` has completed since its last set_fields (host count).
+int pf_batch_steps_done(pf_batch* b, int run) {
+  return (b && run >= 0 && run < b->nruns) ? b->steps_done[run] : -1;
+}
+// Records of steps first .. first+n-1 (0-based, since set_fields) of one run,
+// still in the device ring (n <= the ring length, work complete).
+int pf_batch_records(pf_batch* b, int run, int first, int n, pf_diag* out) {
+  if (!b || run < 0 || run >= b->nruns || n < 0 || n > b->ring || !out) return fail(PF_EINVAL, "bad arguments");
+  PF_CUDA(cudaSetDevice(b->device));
+  std::vector<double> h((size_t)n * DR_COUNT);
+  const double* ring = b->hrp[run].diag;
+  for (int s = 0; s < n;) {
+    const int pos = (first + s) % b->ring, take = std::min(n - s, b->ring - pos);
+    PF_CUDA(cudaMemcpyAsync(h.data() + (size_t)s * DR_COUNT, ring + (size_t)pos * DR_COUNT,
+                            (size_t)take * DR_COUNT * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    s += take;
+  }
+  PF_CUDA(cudaStreamSynchronize(b->stream));
+  for (int s = 0; s < n; ++s) fill_diag(h.data() + (size_t)s * DR_COUNT, &out[s]);
+  return PF_OK;
+}
 // Number of compiled x-pass and yz-pass variants of a grid (the index range
 // of PFGPU_X_VARIANT / PFGPU_YZ_VARIANT).
 void pf_variant_counts(int nx, int ny, int nz, int* nxv, int* nyzv) {

@@ -15,7 +15,8 @@ import numpy as np
 
 from . import build as _build
 
-PF_OK, PF_EINVAL, PF_ECUDA, PF_ENOMEM, PF_ENONFINITE, PF_EIO = 0, -1, -2, -3, -4, -5
+PF_OK, PF_EINVAL, PF_ECUDA, PF_ENOMEM, PF_ENONFINITE, PF_EIO, PF_EBUSY = 0, -1, -2, -3, -4, -5, -6
+PF_REQ_QUEUED, PF_REQ_RUNNING, PF_REQ_DONE, PF_REQ_FAILED = 0, 1, 2, 3
 PF_MOB_REFERENCE, PF_MOB_C1MC = 0, 1
 PF_FP32_FUSED, PF_FP64_PLAIN = 32, 64
 
@@ -27,6 +28,8 @@ EXPORTED = (
     "pf_input_to_config", "pf_write_data_save", "pf_read_data_save", "pf_ic_circle", "pf_ic_plane",
     "pf_ic_polycryst", "pf_insert_precipitates", "pf_format_e", "pf_format_summary", "pf_format_list_int",
     "pf_format_list_real", "pf_analyze_fields", "pf_analyze_run", "pf_write_vtk_real", "pf_write_vtk_int",
+    "pf_server_create", "pf_server_submit", "pf_server_poll", "pf_server_wait", "pf_server_destroy",
+    "pf_server_last_error",
 )
 
 
@@ -85,6 +88,15 @@ class Input(C.Structure):
     @property
     def mobility(self):
         return "c1mc" if self.mobility_code == PF_MOB_C1MC else "reference"
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("max_active", C.c_int), ("hbm_budget_bytes", C.c_double),
+                ("chunk_steps", C.c_int), ("reserved", C.c_int * 5)]
+
+
+class RequestTimes(C.Structure):
+    _fields_ = [("queued_s", C.c_double), ("run_s", C.c_double), ("total_s", C.c_double)]
 
 
 class VoxelCounts(C.Structure):
@@ -165,6 +177,12 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_analyze_run": (C.c_int, [C.c_void_p, C.c_double, P(AnalysisOut), P(VoxelCounts)]),
         "pf_write_vtk_real": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, dp]),
         "pf_write_vtk_int": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, P(C.c_int)]),
+        "pf_server_create": (C.c_int, [P(ServerConfig), P(C.c_void_p)]),
+        "pf_server_submit": (C.c_int, [C.c_void_p, P(Config), dp, dp, C.c_int, P(C.c_longlong)]),
+        "pf_server_poll": (C.c_int, [C.c_void_p, C.c_longlong, ip]),
+        "pf_server_wait": (C.c_int, [C.c_void_p, C.c_longlong, C.c_double, dp, dp, P(Diag), P(RequestTimes)]),
+        "pf_server_destroy": (C.c_int, [C.c_void_p]),
+        "pf_server_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -549,3 +567,66 @@ def variant_counts(nx: int, ny: int, nz: int):
     a, b = C.c_int(0), C.c_int(0)
     load_library().pf_variant_counts(nx, ny, nz, C.byref(a), C.byref(b))
     return a.value, b.value
+
+
+# ---------------------------------------------------------------------------
+# serving: continuous batching of independent runs
+# ---------------------------------------------------------------------------
+class Server:
+    """pf_server: submit runs, poll or wait for them (see include/pfgpu.h)."""
+
+    def __init__(self, device: int = 0, max_active: int = 0, hbm_budget_bytes: float = 0.0, chunk_steps: int = 0):
+        self.lib = load_library()
+        cfg = ServerConfig()
+        cfg.device, cfg.max_active, cfg.hbm_budget_bytes, cfg.chunk_steps = device, max_active, hbm_budget_bytes, \
+            chunk_steps
+        h = C.c_void_p()
+        rc = self.lib.pf_server_create(C.byref(cfg), C.byref(h))
+        if rc != PF_OK:
+            raise PFError(rc, self.lib.pf_server_last_error().decode())
+        self.h = h
+        self.device = device
+        self._shape = {}
+
+    def _check(self, rc):
+        if rc != PF_OK:
+            raise PFError(rc, self.lib.pf_server_last_error().decode())
+
+    def submit(self, params, phi: np.ndarray, con: np.ndarray, nsteps: int) -> int:
+        """Queue a run (fields phi[ivar,z,y,x], con[z,y,x]); returns its id."""
+        cfg = make_config(params, PF_FP32_FUSED, self.device)
+        a = to_aos(phi)
+        c = np.ascontiguousarray(con, dtype=np.float64)
+        rid = C.c_longlong()
+        self._check(self.lib.pf_server_submit(self.h, C.byref(cfg), _dp(a), _dp(c), int(nsteps), C.byref(rid)))
+        self._shape[rid.value] = (params.var, params.Nz, params.Ny, params.Nx)
+        return rid.value
+
+    def poll(self, rid: int) -> int:
+        st = C.c_int()
+        self._check(self.lib.pf_server_poll(self.h, rid, C.byref(st)))
+        return st.value
+
+    def wait(self, rid: int, timeout: float = -1.0):
+        """(phi, con, last record dict, times dict) of a finished run."""
+        var, nz, ny, nx = self._shape.pop(rid)
+        a = np.empty((nz, ny, nx, var))
+        c = np.empty((nz, ny, nx))
+        d = Diag()
+        t = RequestTimes()
+        rc = self.lib.pf_server_wait(self.h, rid, timeout, _dp(a), _dp(c), C.byref(d), C.byref(t))
+        if rc == PF_EBUSY:
+            self._shape[rid] = (var, nz, ny, nx)
+        self._check(rc)
+        return from_aos(a), c, d.as_dict(), {k: getattr(t, k) for k, _ in t._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pf_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -89,3 +89,16 @@ def test_create_without_gpu_fails_cleanly(pkg, oracle):
     with pytest.raises(pkg.PFError) as e:
         pkg.Run(oracle.Params(32, 32, 32, 4))
     assert e.value.code == -2
+
+
+def test_server_create_without_gpu(pkg):
+    """The serving API exists and, without a GPU, refuses to start."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(pkg.PFError) as e:
+        pkg.Server()
+    assert e.value.code == pkg.PF_ECUDA
