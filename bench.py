@@ -339,6 +339,20 @@ def run_ours(args):
             "gpu_launches": kernels_per_step * args.steps,
             "kernel_variants": lib.pf_batch_variant(b).decode(),
         }
+        if ws == 1 and not args.no_fp64:
+            # the plain FP64 GPU path (cuFFT, one kernel per reference phase) on the same workload
+            r64 = pkg.Run(p, precision=pkg.PF_FP64_PLAIN, device=local)
+            r64.set_fields_aos(phi_aos, con)
+            r64.step(2)
+            torch.cuda.synchronize()
+            n64 = 20
+            t64 = time.perf_counter()
+            r64.step(n64, raise_nonfinite=False)
+            t64 = time.perf_counter() - t64
+            r64.close()
+            v64 = cells * p.var * n64 / t64
+            line["fp64_gpu_path"] = {"value": v64, "unit": METRIC, "steps": n64,
+                                     "ratio": value / v64, "what": "PF_FP64_PLAIN, host wall clock per pf_step call"}
         if not args.no_cpu_baseline and ws == 1:
             v, cores, sample, n, dt = cpu_port_throughput(p, 20.0, 50)
             line["cpu_baseline"] = {"value": v, "unit": "cell-steps/s x P", "cores": cores, "kind": "port",
@@ -351,6 +365,181 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# other workloads (not the headline line): the batched ensemble and a served
+# request stream
+# ---------------------------------------------------------------------------
+def _ran2_uniform(pkg, seed: int):
+    """Uniform draws from the reference's ran_2 with idum = -(seed+1)."""
+    r = pkg.Ran2(-(seed + 1))
+    return r.next
+
+
+def ensemble_requests(pkg, n_runs: int, N: int = 64, P: int = 8, seed: int = 3):
+    """Config 3: per run L ~ logU(0.1, 10), kappa ~ U(0.5, 4), g ~ U(1, 2),
+    c0 ~ U(0.3, 0.7), drawn in that order from ran_2 (seed 3); the start of
+    run i is the config-0 noise start from seed 1000*seed + i."""
+    u = _ran2_uniform(pkg, seed)
+    out = []
+    for i in range(n_runs):
+        L = 10 ** (-1 + 2 * u())
+        kap = 0.5 + 3.5 * u()
+        g = 1.0 + u()
+        c0 = 0.3 + 0.4 * u()
+        p = params(Nx=N, Ny=N, Nz=N, var=P, t_step=0.05, mob_phi=L, grad_coeff_phi=kap, grad_coeff_c=kap,
+                   sigma_1=g, sigma_2=g, mobility="reference", D_gb=0.0)
+        out.append((p, 1000 * seed + i, c0))
+    return out
+
+
+def run_ensemble(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    sys.path.insert(0, str(ROOT))
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    lib = pkg.load_library()
+    reqs = ensemble_requests(pkg, args.runs)
+    b = pkg.Batch([r[0] for r in reqs])
+    for i, (p, seed, c0) in enumerate(reqs):
+        phi, con = pkg.ic_noise(p, seed, 0.001, c0, 0.01)
+        b.set_fields(i, phi, con)
+    bh = b.h
+    ext = torch.cuda.ExternalStream(lib.pf_batch_stream(bh), device=0)
+    lib.pf_batch_enqueue(bh, args.warmup)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clocks.mark()
+    e0.record(ext)
+    lib.pf_batch_enqueue(bh, args.steps)
+    e1.record(ext)
+    e1.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    p = reqs[0][0]
+    cells = p.Nx * p.Ny * p.Nz
+    value = cells * p.var * len(reqs) * args.steps / (ms / 1000.0)
+    # the same runs one at a time (a sample), for the gain of batching
+    n1, k1 = min(4, len(reqs)), 100
+    t = 0.0
+    for p1, seed, c0 in reqs[:n1]:
+        run = pkg.Run(p1)
+        phi, con = pkg.ic_noise(p1, seed, 0.001, c0, 0.01)
+        run.set_fields(phi, con)
+        run.step(5)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run.step(k1)
+        t += time.perf_counter() - t0
+        run.close()
+    alone = cells * p.var * n1 * k1 / t
+    nF, Kx = p.var + 1, p.Nx // 2 + 1
+    design_bytes = 6 * nF * Kx * p.Ny * p.Nz * 8 * len(reqs)
+    peak, peak_kind = measured_hbm()
+    achieved = design_bytes / (ms / 1000.0 / args.steps) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (ran_2-seeded noise starts and coefficients)",
+            "config": {"workload": f"ensemble: {len(reqs)} runs of {p.Nx}^3, P={p.var}, one batch (config 3)",
+                       "inputs_vs_l2": "resident working set above L2"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "what": "x + yz pass design bytes of all runs per batched step"},
+            "runs_one_at_a_time": {"value": alone, "unit": METRIC, "runs": n1, "steps": k1},
+            "clocks": clk, "gpu_launches": 3 * args.steps, "kernel_variants": lib.pf_batch_variant(bh).decode()}
+    print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
+def serve_requests(pkg, n: int, rate: float, seed: int = 4):
+    """Config 4: Poisson arrivals at `rate`; grid 32/64/128/256 with
+    probabilities .4/.3/.2/.1, P from {4, 8, 16}, steps ~ logU(100, 5000),
+    coefficients as config 3, all from ran_2 (seed 4)."""
+    import math
+
+    u = _ran2_uniform(pkg, seed)
+    t, out = 0.0, []
+    for i in range(n):
+        t += -math.log(max(u(), 1e-12)) / rate
+        x = u()
+        N = 32 if x < 0.4 else 64 if x < 0.7 else 128 if x < 0.9 else 256
+        P = (4, 8, 16)[min(2, int(3 * u()))]
+        steps = int(round(10 ** (2 + math.log10(50.0) * u())))
+        L, kap, g, c0 = 10 ** (-1 + 2 * u()), 0.5 + 3.5 * u(), 1.0 + u(), 0.3 + 0.4 * u()
+        p = params(Nx=N, Ny=N, Nz=N, var=P, t_step=0.05, mob_phi=L, grad_coeff_phi=kap, grad_coeff_c=kap,
+                   sigma_1=g, sigma_2=g, mobility="reference", D_gb=0.0)
+        out.append((t, p, steps, 4000 * seed + i, c0))
+    return out
+
+
+def _pct(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, int(round(q * (len(xs) - 1))))]
+
+
+def run_serve(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    sys.path.insert(0, str(ROOT))
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    reqs = serve_requests(pkg, args.requests, args.rate)
+    starts = [pkg.ic_noise(p, seed, 0.001, c0, 0.01) for (_, p, _, seed, c0) in reqs]
+    # warm the autotuner cache for every class (as a long-running server would be)
+    for cls in sorted({(p.Nx, p.var) for (_, p, _, _, _) in reqs}):
+        p = next(r[1] for r in reqs if (r[1].Nx, r[1].var) == cls)
+        w = pkg.Run(p)
+        w.close()
+    torch.cuda.synchronize()
+    # served: submit at the arrival times, overlap on the device
+    srv = pkg.Server(max_active=args.max_active)
+    t0 = time.perf_counter()
+    ids = []
+    for (ta, p, steps, _, _), (phi, con) in zip(reqs, starts):
+        while time.perf_counter() - t0 < ta:
+            time.sleep(0.0005)
+        ids.append(srv.submit(p, phi, con, steps))
+    lat = []
+    for i in ids:
+        _, _, _, tm = srv.wait(i)
+        lat.append(tm["total_s"])
+    t_served = time.perf_counter() - t0
+    srv.close()
+    # serial: the same stream, one run at a time in arrival order
+    clock, lat_s = 0.0, []
+    for (ta, p, steps, _, _), (phi, con) in zip(reqs, starts):
+        run = pkg.Run(p)
+        tb = time.perf_counter()
+        run.set_fields(phi, con)
+        run.step(steps, raise_nonfinite=False)
+        run.get_fields()
+        dt = time.perf_counter() - tb
+        run.close()
+        clock = max(clock, ta) + dt
+        lat_s.append(clock - ta)
+    n = len(reqs)
+    work = sum(p.Nx * p.Ny * p.Nz * p.var * steps for (_, p, steps, _, _) in reqs)
+    line = {"metric": "served runs/s", "value": n / t_served, "unit": "runs/s", "n_gpus": 1, "steps": None,
+            "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic request stream (ran_2 seed 4)",
+            "config": {"workload": f"served stream: {n} requests, Poisson rate {args.rate}/s, grids 32-256, "
+                                   f"P 4-16, 100-5000 steps (config 4)", "max_active": args.max_active},
+            "latency_s": {"p50": _pct(lat, 0.5), "p99": _pct(lat, 0.99)},
+            "cell_steps_per_s_x_P": work / t_served,
+            "serial": {"runs_per_s": n / clock, "latency_s": {"p50": _pct(lat_s, 0.5), "p99": _pct(lat_s, 0.99)},
+                       "what": "the same requests one at a time in arrival order (pf_create/pf_step)"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -358,11 +547,22 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU path comparison")
+    ap.add_argument("--workload", choices=["polycrystal", "ensemble", "serve"], default="polycrystal",
+                    help="polycrystal (the headline line), ensemble (config 3) or serve (config 4)")
+    ap.add_argument("--runs", type=int, default=256, help="ensemble: runs in the batch")
+    ap.add_argument("--requests", type=int, default=24, help="serve: requests in the stream")
+    ap.add_argument("--rate", type=float, default=8.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--max-active", type=int, default=16, help="serve: resident runs at most")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

@@ -134,7 +134,7 @@ typedef struct pf_server_config {
   int device;
   int max_active;          /* runs resident at once (0: 64) */
   double hbm_budget_bytes; /* device memory the server's runs may hold (0: 80 % of free memory at create) */
-  int chunk_steps;         /* steps a batch is given at a time (0: 64, at most 1024) */
+  int chunk_steps;         /* steps a batch is given at a time (0: 128, at most 1024) */
   int reserved[5];
 } pf_server_config;
 typedef struct pf_request_times {

@@ -398,13 +398,31 @@ static bool yz_ok(pf_batch* b, const YZKernels& k) {
   return e == cudaSuccess && ncl >= 1;
 }
 
+// Dynamic shared memory a kernel may use is a per-function setting shared by
+// every batch in the process: only ever raise it, so that a batch of fewer
+// fields never lowers it under a live batch of the same grid with more fields.
+static std::mutex g_attr_mu;
+static std::map<std::pair<int, const void*>, int> g_attr_smem;
+static bool raise_smem(const void* fn, size_t bytes) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_attr_mu);
+  int& cur = g_attr_smem[std::make_pair(dev, fn)];
+  if ((int)bytes <= cur) return true;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cur = (int)bytes;
+  return true;
+}
+
 static bool x_ok(pf_batch* b, const XKernels& k) {
   if (b->Ny % k.wy != 0) return false;
   const size_t sm = x_smem(b->Nx, b->nF, k.wy);
   if (sm > kMaxSmem) return false;
   for (KernelFn f : {k.bulk, k.xj, k.imp, k.exp})
-    if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-      return false;
+    if (!raise_smem((const void*)f, sm)) return false;
   return true;
 }
 
@@ -412,8 +430,7 @@ static bool x_ok(pf_batch* b, const XKernels& k) {
 static bool xj_ok(pf_batch* b, const XKernels& k) {
   if (b->Ny % k.wy != 0) return false;
   const size_t sm = x_smem(b->Nx, 1, k.wy);
-  return sm <= kMaxSmem &&
-         cudaFuncSetAttribute((const void*)k.xj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess;
+  return sm <= kMaxSmem && raise_smem((const void*)k.xj, sm);
 }
 
 static void describe_variants(pf_batch* b) {

@@ -10,9 +10,9 @@
 //     same grid, var and mobility class are admitted together as one pf_batch
 //     (one set of launches per step for all of them);
 //   * every resident batch has its own stream and captured step graph; the
-//     worker enqueues a chunk of steps on each batch in turn and comes back
-//     when that chunk is done, so batches of different shapes overlap on the
-//     device while new requests keep arriving;
+//     worker keeps up to two chunks of steps queued on each batch and tops
+//     them up as they complete, so batches of different shapes overlap on the
+//     device, and the device has work while the worker admits new requests;
 //   * a run leaves as soon as its own step count is reached (its fields and
 //     last record are copied out; a batch is freed when all its runs left).
 // Each run computes exactly what it computes alone: the same kernels, per-run
@@ -67,14 +67,21 @@ struct Request {
   Clock::time_point t_submit, t_start, t_done;
 };
 
+struct Chunk {
+  cudaEvent_t ev = nullptr;  // recorded after the chunk's last step
+  int first = 0, n = 0;      // steps first .. first+n-1 (0-based)
+};
+
+constexpr int kInFlight = 2;  // chunks queued per batch, so the GPU has work while the worker is busy
+
 struct Active {
   pf_batch* b = nullptr;
   std::vector<std::shared_ptr<Request>> runs;
-  std::vector<bool> left;    // run finished and copied out
+  std::vector<bool> left;  // run finished and copied out
   size_t bytes = 0;
-  cudaEvent_t ev = nullptr;  // end of the chunk in flight
-  bool in_flight = false;
-  int chunk_first = 0, chunk_n = 0;  // steps of the chunk in flight (0-based)
+  int enq = 0;             // steps enqueued so far (all runs of a batch step together)
+  std::deque<Chunk> flight;
+  std::vector<cudaEvent_t> spare;  // events not in use
 };
 
 }  // namespace
@@ -155,10 +162,15 @@ void admit(pf_server* s) {
     int rc = pf_batch_create(cfgs.data(), (int)cfgs.size(), &a.b);
     for (size_t i = 0; rc == PF_OK && i < group.size(); ++i)
       rc = pf_batch_set_fields(a.b, (int)i, group[i]->phi.data(), group[i]->con.data());
-    if (rc == PF_OK && cudaEventCreateWithFlags(&a.ev, cudaEventDisableTiming) != cudaSuccess) rc = PF_ECUDA;
+    for (int k = 0; rc == PF_OK && k < kInFlight; ++k) {
+      cudaEvent_t ev = nullptr;
+      if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) rc = PF_ECUDA;
+      else a.spare.push_back(ev);
+    }
     if (rc != PF_OK) {
       const std::string msg = pf_last_error();
       if (a.b) pf_batch_destroy(a.b);
+      for (cudaEvent_t ev : a.spare) cudaEventDestroy(ev);
       for (auto& r : group) finish(s, *r, PF_REQ_FAILED, rc, msg);
       continue;
     }
@@ -179,30 +191,51 @@ void admit(pf_server* s) {
   }
 }
 
-// a chunk of `a` has completed: copy out the runs that reached their steps
-void harvest(pf_server* s, Active& a) {
+// The oldest chunk of `a` has completed: take its records and copy out the
+// runs that reached their step count (no later chunk is in flight for them:
+// chunks never run past a member's end).
+void leave(pf_server* s, Active& a, size_t i, int state, int err, const std::string& msg) {
+  a.left[i] = true;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->resident -= 1;
+  }
+  finish(s, *a.runs[i], state, err, msg);
+}
+
+void harvest(pf_server* s, Active& a, const Chunk& c) {
   for (size_t i = 0; i < a.runs.size(); ++i) {
     if (a.left[i]) continue;
     Request& r = *a.runs[i];
-    const int done = pf_batch_steps_done(a.b, (int)i);
-    const int first = a.chunk_first, n = std::min(a.chunk_n, r.nsteps - first);
-    if (n <= 0) continue;
-    std::vector<pf_diag> rec(n);
-    int rc = pf_batch_records(a.b, (int)i, first, n, rec.data());
+    std::vector<pf_diag> rec(c.n);
+    int rc = pf_batch_records(a.b, (int)i, c.first, c.n, rec.data());
     int bad = 0;
     for (const pf_diag& d : rec) bad |= d.nonfinite;
     if (rc == PF_OK && !rec.empty()) r.last = rec.back();
-    if (rc == PF_OK && !bad && done < r.nsteps) continue;  // still running
-    if (rc == PF_OK) rc = pf_batch_get_fields(a.b, (int)i, r.phi.data(), r.con.data());
-    a.left[i] = true;
-    {
-      std::lock_guard<std::mutex> lk(s->mu);
-      s->resident -= 1;
-    }
-    if (rc != PF_OK) finish(s, r, PF_REQ_FAILED, rc, pf_last_error());
-    else if (bad) finish(s, r, PF_REQ_FAILED, PF_ENONFINITE, "a step produced non-finite values");
-    else finish(s, r, PF_REQ_DONE, PF_OK, "");
+    if (rc == PF_OK && !bad && c.first + c.n < r.nsteps) continue;  // still running
+    if (rc == PF_OK && !bad && !a.flight.empty()) continue;          // cannot happen: chunks stop at ends
+    if (rc == PF_OK && !bad) rc = pf_batch_get_fields(a.b, (int)i, r.phi.data(), r.con.data());
+    if (rc != PF_OK) leave(s, a, i, PF_REQ_FAILED, rc, pf_last_error());
+    else if (bad) leave(s, a, i, PF_REQ_FAILED, PF_ENONFINITE, "a step produced non-finite values");
+    else leave(s, a, i, PF_REQ_DONE, PF_OK, "");
   }
+}
+
+// steps the next chunk of `a` may take: up to the nearest member's end
+int next_chunk(const pf_server* s, const Active& a) {
+  int n = s->cfg.chunk_steps;
+  bool any = false;
+  for (size_t i = 0; i < a.runs.size(); ++i)
+    if (!a.left[i]) {
+      any = true;
+      n = std::min(n, a.runs[i]->nsteps - a.enq);
+    }
+  return any ? n : 0;
+}
+
+void fail_rest(pf_server* s, Active& a, int err, const std::string& msg) {
+  for (size_t i = 0; i < a.runs.size(); ++i)
+    if (!a.left[i]) leave(s, a, i, PF_REQ_FAILED, err, msg);
 }
 
 void worker_loop(pf_server* s) {
@@ -216,64 +249,46 @@ void worker_loop(pf_server* s) {
         if (s->stop && s->active.empty()) break;
       }
     }
-    if (!s->stop) admit(s);
     bool progressed = false;
-    for (size_t k = 0; k < s->active.size(); ++k) {
-      Active& a = s->active[k];
-      if (a.in_flight) {
-        if (cudaEventQuery(a.ev) == cudaErrorNotReady) continue;
-        a.in_flight = false;
-        harvest(s, a);
+    for (Active& a : s->active) {
+      // completed chunks, oldest first
+      while (!a.flight.empty() && cudaEventQuery(a.flight.front().ev) != cudaErrorNotReady) {
+        const Chunk c = a.flight.front();
+        a.flight.pop_front();
+        a.spare.push_back(c.ev);
+        harvest(s, a, c);
         progressed = true;
       }
-      // next chunk: up to the nearest member's end, at most chunk_steps
-      int n = s->cfg.chunk_steps, first = -1;
-      for (size_t i = 0; i < a.runs.size(); ++i) {
-        if (a.left[i]) continue;
-        const int done = pf_batch_steps_done(a.b, (int)i);
-        first = done;
-        n = std::min(n, a.runs[i]->nsteps - done);
-      }
-      if (first < 0) continue;  // every run left
-      if (s->stop) {            // shutting down: drop the rest of the work
-        for (size_t i = 0; i < a.runs.size(); ++i)
-          if (!a.left[i]) {
-            a.left[i] = true;
-            {
-              std::lock_guard<std::mutex> lk(s->mu);
-              s->resident -= 1;
-            }
-            finish(s, *a.runs[i], PF_REQ_FAILED, PF_EINVAL, "server destroyed before the run finished");
-          }
+      if (s->stop) {  // shutting down: no new work; what is in flight drains
+        if (a.flight.empty()) fail_rest(s, a, PF_EINVAL, "server destroyed before the run finished");
         continue;
       }
-      n = std::max(1, n);
-      int rc = pf_batch_enqueue(a.b, n);
-      if (rc == PF_OK && cudaEventRecord(a.ev, (cudaStream_t)pf_batch_stream(a.b)) != cudaSuccess) rc = PF_ECUDA;
-      if (rc != PF_OK) {
-        const std::string msg = pf_last_error();
-        for (size_t i = 0; i < a.runs.size(); ++i)
-          if (!a.left[i]) {
-            a.left[i] = true;
-            {
-              std::lock_guard<std::mutex> lk(s->mu);
-              s->resident -= 1;
-            }
-            finish(s, *a.runs[i], PF_REQ_FAILED, rc, msg);
-          }
-        continue;
+      while ((int)a.flight.size() < kInFlight) {
+        const int n = next_chunk(s, a);
+        if (n <= 0) break;
+        Chunk c;
+        c.ev = a.spare.back();
+        c.first = a.enq;
+        c.n = n;
+        int rc = pf_batch_enqueue(a.b, n);
+        if (rc == PF_OK && cudaEventRecord(c.ev, (cudaStream_t)pf_batch_stream(a.b)) != cudaSuccess) rc = PF_ECUDA;
+        if (rc != PF_OK) {
+          fail_rest(s, a, rc, pf_last_error());
+          break;
+        }
+        a.spare.pop_back();
+        a.enq += n;
+        a.flight.push_back(c);
+        progressed = true;
       }
-      a.in_flight = true;
-      a.chunk_first = first;
-      a.chunk_n = n;
-      progressed = true;
     }
+    if (!s->stop) admit(s);
     // free batches whose runs all left
     for (size_t k = 0; k < s->active.size();) {
       Active& a = s->active[k];
-      if (!a.in_flight && std::all_of(a.left.begin(), a.left.end(), [](bool v) { return v; })) {
+      if (a.flight.empty() && std::all_of(a.left.begin(), a.left.end(), [](bool v) { return v; })) {
         pf_batch_destroy(a.b);
-        cudaEventDestroy(a.ev);
+        for (cudaEvent_t ev : a.spare) cudaEventDestroy(ev);
         {
           std::lock_guard<std::mutex> lk(s->mu);
           s->used -= a.bytes;
@@ -284,7 +299,7 @@ void worker_loop(pf_server* s) {
         ++k;
       }
     }
-    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(200));
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(100));
   }
 }
 
@@ -300,7 +315,7 @@ int pf_server_create(const pf_server_config* cfg, pf_server** out) {
   pf_server* s = new pf_server();
   if (cfg) s->cfg = *cfg;
   if (s->cfg.max_active <= 0) s->cfg.max_active = 64;
-  if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 64;
+  if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 128;
   s->cfg.chunk_steps = std::min(s->cfg.chunk_steps, 1024);  // the per-run record ring
   cudaError_t e = cudaSetDevice(s->cfg.device);
   size_t free_b = 0, total_b = 0;

@@ -78,3 +78,24 @@ def test_every_variant_256(pkg, oracle):
             for k in ("f_int", "f_eta", "f_ch", "c_min", "c_max", "phi_min", "phi_P_max"):
                 assert abs(a[k] - b[k]) <= TOL32 * max(1.0, abs(b[k])), (name, a["step"], k, a[k], b[k])
             assert a["nonfinite"] == 0, name
+
+
+def test_runs_of_one_grid_with_different_var_coexist(pkg, oracle):
+    """Kernels are shared by every run of a grid: creating a run with fewer
+    fields must not shrink the shared-memory limit a live run with more fields
+    needs."""
+    pa = oracle.Params(64, 64, 64, 12, t_step=0.05)
+    pb = oracle.Params(64, 64, 64, 3, t_step=0.05)
+    fa = oracle.ic_noise(pa, 1, 0.001, 0.5, 0.01)
+    fb = oracle.ic_noise(pb, 2, 0.001, 0.5, 0.01)
+    ra = pkg.Run(pa)
+    ra.set_fields(*fa)
+    rb = pkg.Run(pb)
+    rb.set_fields(*fb)
+    ra.step(3)
+    rb.step(3)
+    gp, gc = ra.get_fields()
+    ra.close()
+    rb.close()
+    op, oc, _ = oracle.run(pa, fa[0], fa[1], 3, faithful=False, workers=8)
+    _check_fields(gp, gc, op, oc, TOL32)
