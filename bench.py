@@ -330,6 +330,15 @@ def run_ours(args):
                          "other_kernels": {n: {"ms_per_launch": k["ms"], "algorithmic_bytes": k["bytes"],
                                                "GB_s": k["bytes"] / (k["ms"] / 1000.0) / 1e9}
                                            for n, k in kernels.items()}},
+            # the whole step against the reference-shaped byte count per cell-step,
+            # 4 (9P + 21) with variable mobility / 4 (9P + 9) without (FP32 fields;
+            # every 3-D transform one read and one write of its field)
+            "step_roofline": {"bytes_per_cell_step": 4 * (9 * p.var + (21 if var_mob else 9)),
+                              "achieved": 4 * (9 * p.var + (21 if var_mob else 9)) * cells /
+                                          (ms / args.steps / 1000.0) / 1e9,
+                              "peak": peak, "unit": "GB/s",
+                              "frac": 4 * (9 * p.var + (21 if var_mob else 9)) * cells /
+                                      (ms / args.steps / 1000.0) / 1e9 / peak},
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": "cell-steps/s x P",
                     "h2d_bytes_per_step": field_bytes / args.steps,
