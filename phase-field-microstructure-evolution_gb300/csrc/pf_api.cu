@@ -246,7 +246,7 @@ struct pf_batch {
   XKernels xk{};
   XKernels xjk{};              // variant of the xj pass (one field: its best rows per CTA differ)
   YZKernels yk{};
-  size_t smem_x = 0, smem_xj = 0;
+  size_t smem_x = 0, smem_xj = 0, smem_bulk = 0;
   std::vector<RunParams> hrp;
   RunParams* drp = nullptr;
   void* mem = nullptr;         // all per-run buffers
@@ -310,6 +310,31 @@ static int launch_xj(pf_batch* b, cudaStream_t s, int prio = 0) {
   return PF_OK;
 }
 
+// The bulk x pass (one CTA per WY rows, or two-CTA clusters sharing the fields).
+static int launch_x_bulk(pf_batch* b, cudaStream_t s) {
+  const int R = b->nruns;
+  const unsigned nblk = (unsigned)(b->Nz * (b->Ny / b->xk.wy));
+  if (!b->xk.cl) {
+    b->xk.bulk<<<dim3(nblk, R), b->xk.threads, b->smem_bulk, s>>>(b->drp, b->tab.sh);
+    PF_CUDA(cudaGetLastError());
+    return PF_OK;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = b->xk.cl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(b->xk.cl * nblk, R);
+  cfg.blockDim = dim3(b->xk.threads);
+  cfg.dynamicSmemBytes = b->smem_bulk;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  PF_CUDA(cudaLaunchKernelEx(&cfg, b->xk.bulk, (const RunParams*)b->drp, b->tab.sh));
+  return PF_OK;
+}
+
 // One step on stream s.  With `branch` (the captured graph) and variable
 // mobility, the concentration field's chain — its yz planes, the xj pass and
 // the yz C2 pass, which the order-parameter planes do not need — runs on a
@@ -320,8 +345,10 @@ static int launch_xj(pf_batch* b, cudaStream_t s, int prio = 0) {
 static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
   const Shape sh = b->tab.sh;
   const int R = b->nruns;
-  const dim3 gx(b->Nz * (b->Ny / b->xk.wy), R);
-  b->xk.bulk<<<gx, b->xk.threads, b->smem_x, s>>>(b->drp, sh);
+  {
+    const int rc0 = launch_x_bulk(b, s);
+    if (rc0) return rc0;
+  }
   const bool var = b->mob != MOB_CONST;
   if (branch && var && b->side) {
     const int pc = b->V * b->Kx;  // first plane of the c field
@@ -421,8 +448,30 @@ static bool x_ok(pf_batch* b, const XKernels& k) {
   if (b->Ny % k.wy != 0) return false;
   const size_t sm = x_smem(b->Nx, b->nF, k.wy);
   if (sm > kMaxSmem) return false;
-  for (KernelFn f : {k.bulk, k.xj, k.imp, k.exp})
+  if (k.cl) {  // two-CTA bulk: rank 1 must own phi_P and c (var >= 3); the cluster must be schedulable
+    const size_t sb = k.bulk_smem(b->nF);
+    if (b->V < 3 || sb > kMaxSmem || !raise_smem((const void*)k.bulk, sb)) return false;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = k.cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(k.cl * b->Nz * (b->Ny / k.wy), 1);
+    cfg.blockDim = dim3(k.threads);
+    cfg.dynamicSmemBytes = sb;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, (const void*)k.bulk, &cfg) != cudaSuccess || ncl < 1) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  for (KernelFn f : {k.bulk, k.xj, k.imp, k.exp}) {
+    if (k.cl && f == k.bulk) continue;
     if (!raise_smem((const void*)f, sm)) return false;
+  }
   return true;
 }
 
@@ -435,8 +484,8 @@ static bool xj_ok(pf_batch* b, const XKernels& k) {
 
 static void describe_variants(pf_batch* b) {
   char buf[160];
-  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d yz:cluster=%d,threads=%d xj:wy=%d,threads=%d", b->xk.wy,
-           b->xk.threads, b->yk.cluster, b->yk.threads, b->xjk.wy, b->xjk.threads);
+  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d%s yz:cluster=%d,threads=%d xj:wy=%d,threads=%d", b->xk.wy,
+           b->xk.threads, b->xk.cl ? ",cluster=2" : "", b->yk.cluster, b->yk.threads, b->xjk.wy, b->xjk.threads);
   b->variant = buf;
 }
 
@@ -450,6 +499,7 @@ static void apply_variants(pf_batch* b, const XKernels& xk, const YZKernels& yk)
   b->xk = xk;
   b->yk = yk;
   b->smem_x = x_smem(b->Nx, b->nF, xk.wy);
+  b->smem_bulk = xk.cl ? xk.bulk_smem(b->nF) : b->smem_x;
   b->tab.sh.nblk_x = b->Nz * (b->Ny / xk.wy);
   b->tab.sh.nblk_yz = yk.cluster * b->nF * b->Kx;
   apply_xj(b, xk);
@@ -958,7 +1008,8 @@ int pf_batch_enqueue_phase(pf_batch* b, int phase) {
   const Shape sh = b->tab.sh;
   const dim3 gx(b->Nz * (b->Ny / b->xk.wy), b->nruns);
   if (phase == 0) {
-    b->xk.bulk<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp, sh);
+    const int rc = launch_x_bulk(b, b->stream);
+    if (rc) return rc;
   } else {
     int rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, b->nruns, b->stream);
     if (rc) return rc;

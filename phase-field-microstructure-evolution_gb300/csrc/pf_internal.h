@@ -15,6 +15,8 @@ struct XKernels {
   KernelFn bulk, xj, imp, exp;
   int wy;       // y rows per CTA
   int threads;  // threads per CTA
+  int cl = 0;   // 2: the bulk kernel runs as clusters of two CTAs sharing the fields (x_pass_cl_kernel)
+  size_t (*bulk_smem)(int nF) = nullptr;  // its dynamic shared memory (cluster variant)
 };
 
 // ... and of the yz pass (all three modes).

@@ -1156,4 +1156,285 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   }
 }
 
+// ---------------------------------------------------------------------------
+// x pass (bulk mode) split over a cluster of two CTAs.
+//
+// With many order parameters the one-CTA x pass holds (P+1) field rows and
+// fits one CTA per SM.  Here the two CTAs of a cluster take the same WY rows
+// and about half of the fields each (rank 0: fields [0, h), rank 1: [h, P+1),
+// h = ceil((P+1)/2); rank 1 owns phi_P and c), so twice as many CTAs fit an
+// SM.  The cross-field terms need per-cell sums over all fields: each CTA
+// forms partial sums over its own fields (sum phi^2, sum phi^4, pair sum,
+// max |phi|), the pair reads the other's partials through distributed shared
+// memory (pairs = pairs_0 + pairs_1 + pre_0 pre_1), and both derive the same
+// per-cell scalars; rank 1 also writes dF/dc, the mobility and the
+// diagnostics.  Cells whose sum of phi^4 is below 1e-30 take the rescaled
+// branch of bulk_slot with a second exchange (sum of (phi/max|phi|)^4).
+// HBM traffic is that of the one-CTA pass.
+// ---------------------------------------------------------------------------
+template <int NX, int WY>
+struct XCL {
+  static constexpr int M = NX / 2;
+  static constexpr int PM = Line<M>::PITCH;
+  static constexpr int S = WY * M;  // float2 slots (two cells each) per CTA
+  static constexpr int NA = 7;      // per-slot arrays: pre, n4, pairs, mabs (partials), nn (partial), phiP, c
+  static constexpr size_t smem(int nF) { return ((size_t)((nF + 1) / 2) * WY * PM + (size_t)NA * S) * sizeof(float2); }
+};
+
+struct CellOut {
+  float t4a, t4p, invm, dc, mb;
+  int bad;
+};
+
+// per-cell scalars of bulk_slot from the full aggregates of one cell
+__device__ __forceinline__ CellOut cell_terms(float pp, float c, float pre, float n4, float pairs, float mabs, float nn,
+                                              const RunParams& rp, BulkAcc& acc) {
+  const float pp2 = pp * pp;
+  const float S2 = pre + pp2;
+  const float S4 = n4 + pp2 * pp2;
+  float invS4, n4n, sc, im = 1.f;
+  if (S4 >= 1e-30f) {
+    invS4 = 1.f / S4;
+    n4n = n4 * invS4;
+    sc = 4.f;
+  } else if (mabs > 0.f) {
+    im = 1.f / mabs;
+    const float xq = pp * im;
+    const float s4 = nn + (xq * xq) * (xq * xq);
+    invS4 = 1.f / s4;
+    n4n = nn * invS4;
+    sc = 4.f * im;
+  } else {
+    invS4 = 0.f;
+    n4n = 0.f;
+    sc = 0.f;
+  }
+  const float h = n4n;
+  const float dcm = c - rp.c0m, dcp = c - rp.c0p;
+  const float fm = rp.am * dcm * dcm, fp = rp.ap * dcp * dcp;
+  const float dfm = fm - fp;
+  acc.fch += h * fm + (1.f - h) * fp;
+  CellOut o;
+  o.dc = 2.f * h * rp.am * dcm + 2.f * (1.f - h) * rp.ap * dcp;
+  acc.feta += -0.5f * S2 + 0.25f * S4 + rp.sigma1 * pairs + rp.sigma2 * pp2 * pre;
+  acc.mass += c;
+  acc.cmin = fminf(acc.cmin, c);
+  acc.cmax = fmaxf(acc.cmax, c);
+  acc.phimin = fminf(acc.phimin, S2);
+  acc.phipmax = fmaxf(acc.phipmax, pp);
+  if (rp.mobility == MOB_REF_VAR) o.mb = 2.f * (1.f - S2) * rp.D_gb;
+  else if (rp.mobility == MOB_C1MC) o.mb = rp.D_L * c * (1.f - c);
+  else o.mb = 0.f;
+  const float qP = pp * im;
+  const float qP2 = qP * qP;
+  const float rP4 = qP2 * qP2 * invS4;
+  o.t4a = sc * invS4 * rP4 * dfm;
+  o.t4p = -sc * (qP * qP2 * invS4) * n4n * dfm;
+  o.invm = im;
+  o.bad = !isfinite(S4 + S2 + pairs + o.dc + o.t4a + o.t4p);
+  return o;
+}
+
+template <int NX, int WY, int T>
+__global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restrict__ runs, const Shape sh) {
+  using G = XCL<NX, WY>;
+  constexpr int M = G::M, PM = G::PM, S = G::S;
+  using LM = Line<M>;
+  constexpr int NP = LM::N2 / 2 + 1;
+  static_assert(LM::N2 % 2 == 0, "x plan needs an even number of runs");
+  enum { A_PRE = 0, A_N4, A_PAIRS, A_MABS, A_NN, A_PP, A_C };
+  extern __shared__ float2 smem[];
+  const RunParams& rp = runs[blockIdx.y];
+  const int V = rp.V, nF = V + 1, h = (nF + 1) / 2;
+  const int rank = (int)(blockIdx.x & 1), peer = rank ^ 1, bp = (int)(blockIdx.x >> 1);
+  const int fbase = rank ? h : 0, nloc = rank ? nF - h : h;
+  const int ny_tiles = sh.Ny / WY;
+  const int z = bp / ny_tiles;
+  const int y0 = (bp - z * ny_tiles) * WY;
+  const size_t plane = (size_t)sh.Nz * sh.Ny;
+  const size_t fstride = (size_t)sh.Kx * plane;
+  const size_t row_off = (size_t)z * sh.Ny + y0;
+  float2* lines = smem;                          // nloc * WY lines
+  float2* A = smem + (size_t)h * WY * PM;        // the same offset in both CTAs
+  const uint32_t peer_A = map_rank(smem_addr(A), peer);
+  const uint32_t peer_lines = map_rank(smem_addr(lines), peer);
+
+  // 1. inverse x transform of the local fields
+  for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
+    const int l = it % (nloc * WY), pr = it / (nloc * WY);
+    const int fl = l / WY, yy = l - fl * WY;
+    x_inv_runs<M>(rp.Sm + (fbase + fl) * fstride + row_off + yy, plane, lines + l * PM, pr, sh.twN);
+  }
+  __syncthreads();
+  passA_rt<M, PM, T, true>(lines, nloc * WY, sh.twM);
+  __syncthreads();
+
+  // 2. partial sums over the local matrix fields (f < V-1), in field order
+  const int fend = min(fbase + nloc, V - 1);
+  for (int it = threadIdx.x; it < S; it += T) {
+    const int m = it % M, yy = it / M;
+    const float2* base = lines + yy * PM + LM::phys(m);
+    float pre0 = 0.f, pre1 = 0.f, n40 = 0.f, n41 = 0.f, pr0 = 0.f, pr1 = 0.f, ma0 = 0.f, ma1 = 0.f;
+    for (int f = fbase; f < fend; ++f) {
+      const float2 p = base[(f - fbase) * WY * PM];
+      const float a0 = p.x * p.x, a1 = p.y * p.y;
+      pr0 = fmaf(a0, pre0, pr0);
+      pr1 = fmaf(a1, pre1, pr1);
+      pre0 += a0;
+      pre1 += a1;
+      n40 = fmaf(a0, a0, n40);
+      n41 = fmaf(a1, a1, n41);
+      ma0 = fmaxf(ma0, fabsf(p.x));
+      ma1 = fmaxf(ma1, fabsf(p.y));
+    }
+    A[A_PRE * S + it] = make_float2(pre0, pre1);
+    A[A_N4 * S + it] = make_float2(n40, n41);
+    A[A_PAIRS * S + it] = make_float2(pr0, pr1);
+    A[A_MABS * S + it] = make_float2(ma0, ma1);
+  }
+  cluster_barrier<2>();
+
+  // full sums (rank 0's part first in both CTAs: both get the same bits)
+  auto totals = [&](int it, float2& pre, float2& n4, float2& pairs, float2& mabs) {
+    float2 a[4], b[4];  // rank 0's and rank 1's partials
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float2 own = A[k * S + it];
+      const float2 oth = ld_peer<2>(peer_A + (uint32_t)((k * S + it) * 8));
+      a[k] = rank ? oth : own;
+      b[k] = rank ? own : oth;
+    }
+    pre = make_float2(a[0].x + b[0].x, a[0].y + b[0].y);
+    n4 = make_float2(a[1].x + b[1].x, a[1].y + b[1].y);
+    pairs = make_float2(fmaf(a[0].x, b[0].x, a[2].x + b[2].x), fmaf(a[0].y, b[0].y, a[2].y + b[2].y));
+    mabs = make_float2(fmaxf(a[3].x, b[3].x), fmaxf(a[3].y, b[3].y));
+  };
+
+  // 3. phi_P and c from rank 1; the rescaled sum where a cell needs it
+  for (int it = threadIdx.x; it < S; it += T) {
+    const int m = it % M, yy = it / M;
+    const int off_p = ((V - 1 - h) * WY + yy) * PM + LM::phys(m);  // in rank 1's lines
+    const int off_c = ((V - h) * WY + yy) * PM + LM::phys(m);
+    float2 pP, cc;
+    if (rank) {
+      pP = lines[off_p];
+      cc = lines[off_c];
+    } else {
+      pP = ld_peer<2>(peer_lines + (uint32_t)(off_p * 8));
+      cc = ld_peer<2>(peer_lines + (uint32_t)(off_c * 8));
+    }
+    A[A_PP * S + it] = pP;
+    A[A_C * S + it] = cc;
+    float2 pre, n4, pairs, mabs;
+    totals(it, pre, n4, pairs, mabs);
+    float nn[2] = {0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const float pp = q ? pP.y : pP.x;
+      const float S4 = (q ? n4.y : n4.x) + (pp * pp) * (pp * pp);
+      const float ma = fmaxf(q ? mabs.y : mabs.x, fabsf(pp));
+      if (S4 < 1e-30f && ma > 0.f) {
+        const float im = 1.f / ma;
+        const float2* base = lines + yy * PM + LM::phys(m);
+        for (int f = fbase; f < fend; ++f) {
+          const float2 p = base[(f - fbase) * WY * PM];
+          const float x = (q ? p.y : p.x) * im;
+          nn[q] = fmaf(x * x, x * x, nn[q]);
+        }
+      }
+    }
+    A[A_NN * S + it] = make_float2(nn[0], nn[1]);
+  }
+  cluster_barrier<2>();
+
+  // 4. per-cell scalars and dF of the local fields, in place
+  BulkAcc acc;
+  acc.feta = 0.f; acc.fch = 0.f; acc.mass = 0.f;
+  acc.cmin = 1.0f; acc.cmax = 0.0f; acc.phimin = 1.0f; acc.phipmax = 0.0f;  // reference start values
+  acc.nonfinite = 0;
+  const float sg1 = rp.sigma1, sg2 = rp.sigma2;
+  for (int it = threadIdx.x; it < S; it += T) {
+    const int m = it % M, yy = it / M;
+    float2 pre, n4, pairs, mabs;
+    totals(it, pre, n4, pairs, mabs);
+    const float2 pP = A[A_PP * S + it], cc = A[A_C * S + it];
+    const float2 own_nn = A[A_NN * S + it];
+    const float2 oth_nn = ld_peer<2>(peer_A + (uint32_t)((A_NN * S + it) * 8));
+    const float2 nn0 = rank ? oth_nn : own_nn, nn1 = rank ? own_nn : oth_nn;
+    CellOut o[2];
+    o[0] = cell_terms(pP.x, cc.x, pre.x, n4.x, pairs.x, fmaxf(mabs.x, fabsf(pP.x)), nn0.x + nn1.x, rp, acc);
+    o[1] = cell_terms(pP.y, cc.y, pre.y, n4.y, pairs.y, fmaxf(mabs.y, fabsf(pP.y)), nn0.y + nn1.y, rp, acc);
+    float2* base = lines + yy * PM + LM::phys(m);
+    for (int f = fbase; f < fbase + nloc; ++f) {
+      float2& slot = base[(f - fbase) * WY * PM];
+      float2 d;
+      if (f < V - 1) {
+        const float2 p = slot;
+        const float g0 = fmaf(sg1, pre.x - p.x * p.x, sg2 * (pP.x * pP.x));
+        const float g1 = fmaf(sg1, pre.y - p.y * p.y, sg2 * (pP.y * pP.y));
+        const float q0 = p.x * o[0].invm, q1 = p.y * o[1].invm;
+        d.x = fmaf(p.x, p.x * p.x, -p.x) + 2.f * p.x * g0 + o[0].t4a * (q0 * q0 * q0);
+        d.y = fmaf(p.y, p.y * p.y, -p.y) + 2.f * p.y * g1 + o[1].t4a * (q1 * q1 * q1);
+      } else if (f == V - 1) {
+        d.x = fmaf(pP.x, pP.x * pP.x, -pP.x) + 2.f * pP.x * (sg2 * pre.x) + o[0].t4p;
+        d.y = fmaf(pP.y, pP.y * pP.y, -pP.y) + 2.f * pP.y * (sg2 * pre.y) + o[1].t4p;
+      } else {
+        d = make_float2(o[0].dc, o[1].dc);
+      }
+      slot = d;
+    }
+    if (rank && rp.mobility != MOB_CONST)
+      *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = make_float2(o[0].mb, o[1].mb);
+    acc.nonfinite += o[0].bad | o[1].bad;
+  }
+  cluster_barrier<2>();  // no distributed-shared-memory access after this point
+
+  // 5. forward x transform of the local fields -> D
+  passA_rt<M, PM, T, false>(lines, nloc * WY, sh.twM);
+  __syncthreads();
+  const float scale = 1.0f / (float)NX;
+  for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
+    const int l = it % (nloc * WY), pr = it / (nloc * WY);
+    const int fl = l / WY, yy = l - fl * WY;
+    x_fwd_runs<M>(rp.D + (fbase + fl) * fstride + row_off + yy, plane, lines + l * PM, pr, scale, sh.twN);
+  }
+  if (!rank) return;
+
+  // 6. diagnostics (rank 1): block reduction into the pair's partials
+  __shared__ double red_d[3][T / 32];
+  __shared__ float red_f[4][T / 32];
+  __shared__ int red_i[T / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double s0 = warp_sum((double)acc.feta), s1 = warp_sum((double)acc.fch), s2 = warp_sum((double)acc.mass);
+  float m0 = warp_min(acc.cmin), m1 = warp_max(acc.cmax), m2 = warp_min(acc.phimin), m3 = warp_max(acc.phipmax);
+  int nb = __reduce_add_sync(0xffffffffu, acc.nonfinite);
+  if (lane == 0) {
+    red_d[0][wid] = s0; red_d[1][wid] = s1; red_d[2][wid] = s2;
+    red_f[0][wid] = m0; red_f[1][wid] = m1; red_f[2][wid] = m2; red_f[3][wid] = m3;
+    red_i[wid] = nb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a0 = 0, a1 = 0, a2 = 0;
+    float b0 = red_f[0][0], b1 = red_f[1][0], b2 = red_f[2][0], b3 = red_f[3][0];
+    int nn = 0;
+    for (int w = 0; w < T / 32; ++w) {
+      a0 += red_d[0][w]; a1 += red_d[1][w]; a2 += red_d[2][w];
+      b0 = fminf(b0, red_f[0][w]); b1 = fmaxf(b1, red_f[1][w]);
+      b2 = fminf(b2, red_f[2][w]); b3 = fmaxf(b3, red_f[3][w]);
+      nn += red_i[w];
+    }
+    const int nbk = sh.nblk_x;
+    double* p = rp.part_x + bp;
+    p[XD_FETA * nbk] = a0;
+    p[XD_FCH * nbk] = a1;
+    p[XD_MASS * nbk] = a2;
+    p[XD_CMIN * nbk] = b0;
+    p[XD_CMAX * nbk] = b1;
+    p[XD_PHIMIN * nbk] = b2;
+    p[XD_PHIPMAX * nbk] = b3;
+    p[XD_NONFINITE * nbk] = nn;
+  }
+}
+
 }  // namespace pf

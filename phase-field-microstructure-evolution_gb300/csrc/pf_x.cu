@@ -15,22 +15,53 @@ static int add(XKernels* out, int n) {
   k.exp = x_pass_kernel<NX, WY, T, MODE_EXPORT>;
   k.wy = WY;
   k.threads = T;
+  k.cl = 0;
+  k.bulk_smem = nullptr;
   return n + 1;
+}
+
+template <int NX, int WY>
+static size_t cl_smem(int nF) {
+  return XCL<NX, WY>::smem(nF);
+}
+
+// bulk pass split over two-CTA clusters; the other modes use the one-CTA kernel
+template <int NX, int WY, int T>
+static int addcl(XKernels* out, int n) {
+  if (n >= kMaxVariants) return n;
+  n = add<NX, WY, T>(out, n);
+  XKernels& k = out[n - 1];
+  k.bulk = x_pass_cl_kernel<NX, WY, T>;
+  k.cl = 2;
+  k.bulk_smem = cl_smem<NX, WY>;
+  return n;
 }
 
 int x_variants_a(int nx, XKernels* out, int n) {
   switch (nx) {
     case 16: n = add<16, 16, 256>(out, n); break;
     case 32: n = add<32, 16, 256>(out, n); n = add<32, 8, 128>(out, n); break;
-    case 64: n = add<64, 8, 256>(out, n); n = add<64, 16, 256>(out, n); n = add<64, 4, 128>(out, n); break;
-    case 96: n = add<96, 8, 256>(out, n); n = add<96, 4, 256>(out, n); n = add<96, 16, 256>(out, n); break;
+    case 64:
+      n = add<64, 8, 256>(out, n); n = add<64, 16, 256>(out, n); n = add<64, 4, 128>(out, n);
+      n = addcl<64, 8, 256>(out, n);
+      break;
+    case 96:  // 512-thread CTAs keep 16 warps per SM when many fields leave room for one CTA only
+      n = add<96, 8, 256>(out, n); n = add<96, 4, 256>(out, n); n = add<96, 16, 256>(out, n);
+      n = add<96, 4, 512>(out, n); n = add<96, 8, 512>(out, n);
+      n = addcl<96, 4, 256>(out, n); n = addcl<96, 8, 256>(out, n);
+      break;
     case 128:
       n = add<128, 8, 256>(out, n);
       n = add<128, 4, 256>(out, n);
       n = add<128, 4, 128>(out, n);
       n = add<128, 16, 256>(out, n);
+      n = add<128, 4, 512>(out, n);
+      n = addcl<128, 4, 256>(out, n); n = addcl<128, 8, 256>(out, n);
       break;
-    case 256: n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n); break;
+    case 256:
+      n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n);
+      n = addcl<256, 4, 256>(out, n); n = addcl<256, 4, 512>(out, n);
+      break;
     default: break;
   }
   return n;
