@@ -52,6 +52,29 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, dist=None, device: str = "cpu") -> float:
+    """The largest value of x over the ranks of the process group (x itself
+    without one): whole-job times are the slowest rank's."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(cells: int, P: int, steps: int, ranks: int, seconds: float) -> float:
+    """Whole-job cell-steps/s x P: every rank steps its own replica of
+    `cells` cells and P order parameters `steps` times in `seconds`."""
+    return cells * P * steps * ranks / seconds
+
+
+def replica_seed(rank: int) -> int:
+    """Voronoi seed of rank's replica (independent runs, no collective)."""
+    return IC["seed"] + rank
+
+
 class Clocks:
     """nvidia-smi sampler running during the timed region."""
 
@@ -228,7 +251,7 @@ def run_ours(args):
     Kx = p.Nx // 2 + 1
     var_mob = p.mobility == "c1mc" or p.D_gb != 0.0
 
-    phi_aos, con = pkg.ic_voronoi_aos(p, IC["seed"] + rank, IC["n_grains"], IC["amp_phi"], IC["c0"], IC["amp_c"],
+    phi_aos, con = pkg.ic_voronoi_aos(p, replica_seed(rank), IC["n_grains"], IC["amp_phi"], IC["c0"], IC["amp_c"],
                                       pinned=True)
     run = pkg.Run(p, device=local)
     run.set_fields_aos(phi_aos, con)
@@ -264,11 +287,8 @@ def run_ours(args):
     d = run.step(1)[0]
     if d["nonfinite"]:
         raise RuntimeError("non-finite values in the benchmark run")
-    if dist is not None:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = cells * p.var * args.steps * ws / (ms / 1000.0)
+    ms = max_over_ranks(ms, dist, f"cuda:{local}")
+    value = job_throughput(cells, p.var, args.steps, ws, ms / 1000.0)
 
     # per-kernel timing on the same stream (each kernel alone, back to back)
     plane = p.Ny * p.Nz * Kx * 8  # bytes of one field's half spectrum (complex64)
@@ -309,11 +329,8 @@ def run_ours(args):
     run.get_fields_aos(out_phi, out_con)
     t1 = time.perf_counter()
     e2e_s = t1 - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = cells * p.var * args.steps * ws / e2e_s
+    e2e_s = max_over_ranks(e2e_s, dist, f"cuda:{local}")
+    e2e_value = job_throughput(cells, p.var, args.steps, ws, e2e_s)
     field_bytes = (phi_aos.nbytes + con.nbytes)
     diag_bytes = 80  # sizeof(pf_diag)
     assert len(recs) == args.steps
