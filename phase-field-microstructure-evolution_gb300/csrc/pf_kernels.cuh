@@ -87,6 +87,14 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// FP32 warp sum: the per-warp partials of the diagnostics (32 FP32 thread
+// sums) are then added in FP64 per block and across blocks; FP64 arithmetic
+// is scarce on this part, FP32 shuffles are not.
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 __device__ __forceinline__ float warp_min(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -567,6 +575,98 @@ struct YZ {
 
 enum YZMode { YZ_MAIN = 0, YZ_C2 = 1, YZ_IMPORT = 2 };
 
+// ---------------------------------------------------------------------------
+// Pointwise semi-implicit update of one k-point, shared by both yz kernels.
+// The reference's forms (var_diff.f90 lines cited at the call sites)
+//   AC: u += (-L dt kappa q^2 u - L dt D) / (1 + L dt kappa q^2)
+//   CH: c += (-D dt kappa_c K4 c - D dt q^2 mu) / (1 + D dt kappa_c K4)
+// are evaluated in the algebraically equal folded form u' = (u - b D) /
+// (1 + a Q), Q = q^2 (AC) or K4 (CH), with the 1/(NY NZ) normalisation of the
+// transform folded into b, and the single-precision fast reciprocal (about
+// 2 ulp, far below the step's own FP32 rounding).  The kz factors come from a
+// shared-memory table {qz^2, qz^4, qn_z, qn_z^2} staged once per CTA.
+// ---------------------------------------------------------------------------
+template <int NZ, int T>
+__device__ __forceinline__ void stage_kz(float4* qt, const Shape& sh) {
+  for (int k = threadIdx.x; k < NZ; k += T) {
+    const float n = __ldg(sh.qnz + k);
+    qt[k] = make_float4(__ldg(sh.qz2 + k), __ldg(sh.qz4 + k), n, n * n);
+  }
+}
+
+struct KPlane {
+  float qx2, qx4, qnx;
+  float a;    // slope of the denominator in Q
+  float b;    // coefficient of the driving term, normalisation included
+  float nrm;  // 1 / (NY NZ)
+  float kc;   // kappa_c
+  __device__ __forceinline__ KPlane(const RunParams& rp, const Shape& sh, int kx, int mode, bool is_c, float nrm_) {
+    qx2 = sh.qx2[kx];
+    qx4 = sh.qx4[kx];
+    qnx = sh.qnx[kx];
+    nrm = nrm_;
+    kc = rp.kappa_c;
+    if (mode == YZ_MAIN && !is_c) {
+      a = rp.L * rp.dt * rp.kappa_phi;
+      b = rp.L * rp.dt * nrm_;
+    } else {
+      a = rp.D_L * rp.dt * rp.kappa_c;
+      b = (mode == YZ_MAIN ? rp.D_L * rp.dt : rp.dt) * nrm_;
+    }
+  }
+};
+
+// the kx + ky parts of the k-point factors of one y position
+struct KRow {
+  float q2, q4, n2, g, k3;
+  __device__ __forceinline__ KRow(const KPlane& P, const Shape& sh, int ky) {
+    const float qy2 = __ldg(sh.qy2 + ky), qy4 = __ldg(sh.qy4 + ky), qny = __ldg(sh.qny + ky);
+    q2 = P.qx2 + qy2;
+    q4 = P.qx4 + qy4;
+    n2 = fmaf(P.qnx, P.qnx, qny * qny);
+    g = P.qnx + qny;
+    k3 = fmaf(P.qnx, P.qx2, qny * qy2);
+  }
+};
+
+// u: the k-space state (in: old, out: new); d: the unnormalised transform of
+// the driving term (MAIN: dF/dphi or mu; C2: J'), on return J_hat where the
+// c plane of a variable-mobility run hands it to the inverse transform.
+template <int MODE>
+__device__ __forceinline__ void kpoint(const KPlane& P, const KRow& R, const float4 z, const bool is_c, const bool var_c,
+                                       float2& u, float2& d, float& fint) {
+  if (MODE == YZ_IMPORT) {
+    u = make_float2(d.x * P.nrm, d.y * P.nrm);
+    return;
+  }
+  const float2 uu = u;
+  const float q2 = R.q2 + z.x;
+  if (MODE == YZ_MAIN) {
+    // f_int by Parseval: |kf|^2 |u_hat|^2
+    fint = fmaf(R.n2 + z.w, fmaf(uu.x, uu.x, uu.y * uu.y), fint);
+    if (!is_c) {
+      // AC (:1015-1024)
+      const float inv = __fdividef(1.0f, fmaf(P.a, q2, 1.0f));
+      u = make_float2(fmaf(-P.b, d.x, uu.x) * inv, fmaf(-P.b, d.y, uu.y) * inv);
+    } else {
+      // CH (:976-983), K2 = -q^2
+      const float inv = __fdividef(1.0f, fmaf(P.a, R.q4 + z.y, 1.0f));
+      const float bq = P.b * q2;
+      u = make_float2(fmaf(-bq, d.x, uu.x) * inv, fmaf(-bq, d.y, uu.y) * inv);
+      if (var_c) {
+        // J_hat = G mu_hat - kappa_c c_hat K3 (:932-935), G = i g, K3 = -i (qn . q^2)
+        const float gn = (R.g + z.z) * P.nrm;
+        const float kk = P.kc * fmaf(z.z, z.x, R.k3);
+        d = cmul_pi(make_float2(fmaf(gn, d.x, kk * uu.x), fmaf(gn, d.y, kk * uu.y)));
+      }
+    }
+  } else {
+    // C2: c += dt G J'_hat / (1 + D dt kappa_c K4)  (:976)
+    const float sg = __fdividef(P.b * (R.g + z.z), fmaf(P.a, R.q4 + z.y, 1.0f));
+    u = cadd(uu, cmul_pi(make_float2(d.x * sg, d.y * sg)));
+  }
+}
+
 template <int C>
 __device__ __forceinline__ void cluster_barrier() {
   if constexpr (C == 1) {
@@ -723,6 +823,8 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   static_assert(T % N1y == 0 && T % N2z == 0, "thread count");
   extern __shared__ float2 smem[];
   __shared__ double red[T / 32];
+  __shared__ float4 qzt[NZ];  // kz factors of the k-space update
+  stage_kz<NZ, T>(qzt, sh);   // read after the barriers of the forward passes
   float2* UA = smem;
   float2* UB = smem + G::UA;
   const RunParams& rp = runs[blockIdx.y];
@@ -773,8 +875,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
 
   // 2. last forward z pass, pointwise k-space update, first inverse z pass,
   //    fused per run of N1z positions
-  const float inv_nyz = 1.0f / (float)(NY * NZ);
-  const float qx2 = sh.qx2[kx], qx4 = sh.qx4[kx], qnx = sh.qnx[kx];
+  const KPlane P(rp, sh, kx, MODE, is_c, 1.0f / (float)(NY * NZ));
   const float wkx = (kx == 0 || 2 * kx == sh.Nx) ? 1.0f : 2.0f;
   float fint = 0.f;
   {
@@ -786,8 +887,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
       if (ITEMS % T != 0 && it >= ITEMS) break;
       const int yl = it / N2z;
       const int ypos = r * G::LB + yl;
-      const int ky = LY::freq_of_pos(ypos);
-      const float qy2 = __ldg(sh.qy2 + ky), qy4 = __ldg(sh.qy4 + ky), qn_y = __ldg(sh.qny + ky);
+      const KRow R(P, sh, LY::freq_of_pos(ypos));
       float2* pb = UB + yl * G::PZ + k2 * (N1z + 1);
       // k-space state of this plane in [k1][y position][k2] order: for every
       // k1 a warp reads and writes consecutive (y position, k2) (coalesced)
@@ -802,54 +902,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
         for (int k1 = 0; k1 < N1z; ++k1) u[k1] = gk[k1 * SK1];
       }
 #pragma unroll
-      for (int k1 = 0; k1 < N1z; ++k1) {
-        const int kz = k2 + N2z * k1;
-        const float2 dd = make_float2(d[k1].x * inv_nyz, d[k1].y * inv_nyz);  // normalised D_hat
-        if (MODE == YZ_IMPORT) {
-          u[k1] = dd;
-          continue;
-        }
-        const float q2 = qx2 + qy2 + __ldg(sh.qz2 + kz);
-        const float qn_z = __ldg(sh.qnz + kz);
-        const float2 uu = u[k1];
-        if (MODE == YZ_MAIN) {
-          const float kn2 = qnx * qnx + qn_y * qn_y + qn_z * qn_z;
-          fint = fmaf(kn2, uu.x * uu.x + uu.y * uu.y, fint);
-          if (!is_c) {
-            // AC (:1015-1024): u += (-L dt kappa q^2 u - L dt D) / (1 + L kappa dt q^2)
-            const float lk = rp.L * rp.dt;
-            const float den = fmaf(lk * rp.kappa_phi, q2, 1.0f);
-            const float inv = 1.0f / den;
-            const float m1 = -lk * rp.kappa_phi * q2 * inv;
-            const float m2 = -lk * inv;
-            u[k1] = make_float2(uu.x + fmaf(m1, uu.x, m2 * dd.x), uu.y + fmaf(m1, uu.y, m2 * dd.y));
-          } else {
-            // CH (:976-983): c += (-D dt kappa_c K4 c + D K2 dt mu) / (1 + D dt kappa_c K4), K2 = -q^2
-            const float q4 = qx4 + qy4 + __ldg(sh.qz4 + kz);
-            const float dm = rp.D_L * rp.dt;
-            const float den = fmaf(dm * rp.kappa_c, q4, 1.0f);
-            const float inv = 1.0f / den;
-            const float m1 = -dm * rp.kappa_c * q4 * inv;
-            const float m2 = -dm * q2 * inv;
-            u[k1] = make_float2(uu.x + fmaf(m1, uu.x, m2 * dd.x), uu.y + fmaf(m1, uu.y, m2 * dd.y));
-            if (var_c) {
-              // J_hat = G mu_hat - kappa_c c_hat K3 (:932-935), G = i g, K3 = i k3;
-              // the d registers carry J_hat to the inverse transform
-              const float g = qnx + qn_y + qn_z;
-              const float k3 = -(qnx * qx2 + qn_y * qy2 + qn_z * __ldg(sh.qz2 + kz));
-              d[k1] = cmul_pi(make_float2(g * dd.x - rp.kappa_c * k3 * uu.x, g * dd.y - rp.kappa_c * k3 * uu.y));
-            }
-          }
-        } else {
-          // C2: c += dt G J'_hat / (1 + D dt kappa_c K4)  (:976)
-          const float q4 = qx4 + qy4 + __ldg(sh.qz4 + kz);
-          const float dm = rp.D_L * rp.dt;
-          const float den = fmaf(dm * rp.kappa_c, q4, 1.0f);
-          const float g = qnx + qn_y + qn_z;
-          const float s = rp.dt * g / den;
-          u[k1] = cadd(uu, cmul_pi(make_float2(dd.x * s, dd.y * s)));
-        }
-      }
+      for (int k1 = 0; k1 < N1z; ++k1) kpoint<MODE>(P, R, qzt[k2 + N2z * k1], is_c, var_c, u[k1], d[k1], fint);
 #pragma unroll
       for (int k1 = 0; k1 < N1z; ++k1) gk[k1 * SK1] = u[k1];
       if (MODE != YZ_IMPORT) {
@@ -910,7 +963,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
 
   if (MODE == YZ_MAIN) {
     // f_int partial (:609-678 by Parseval): 0.5 kappa N^3 w |kf|^2 |u_hat|^2
-    double v = warp_sum((double)fint);
+    const double v = (double)warp_sumf(fint);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) red[wid] = v;
     __syncthreads();
@@ -976,6 +1029,8 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   static_assert(T % N1y == 0 && T % N2y == 0, "thread count");
   extern __shared__ float2 U[];
   __shared__ double red[T / 32];
+  __shared__ float4 qzt[NZ];  // kz factors of the k-space update
+  stage_kz<NZ, T>(qzt, sh);   // read after the barriers of the forward passes
   const RunParams& rp = runs[blockIdx.y];
   const int p = sh.plane0 + (int)blockIdx.x;
   const int Kx = sh.Kx;
@@ -1017,8 +1072,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   __syncthreads();
 
   // 2. last forward z pass, pointwise k-space update, first inverse z pass
-  const float inv_nyz = 1.0f / (float)(NY * NZ);
-  const float qx2 = sh.qx2[kx], qx4 = sh.qx4[kx], qnx = sh.qnx[kx];
+  const KPlane P(rp, sh, kx, MODE, is_c, 1.0f / (float)(NY * NZ));
   const float wkx = (kx == 0 || 2 * kx == sh.Nx) ? 1.0f : 2.0f;
   float fint = 0.f;
   {
@@ -1028,12 +1082,11 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
       const int it = threadIdx.x + j * T;
       if (ITEMS % T != 0 && it >= ITEMS) break;
       const int yp = it % NY, k2 = it / NY;
-      const int ky = LY::freq_of_pos(yp);
-      const float qy2 = __ldg(sh.qy2 + ky), qy4 = __ldg(sh.qy4 + ky), qn_y = __ldg(sh.qny + ky);
+      const KRow R(P, sh, LY::freq_of_pos(yp));
       float2* pc = U + (k2 * N1z) * PY + LY::phys(yp);
       // k-space state of this plane in [k1][k2][y position] order: for every
       // k1 a warp reads and writes 32 consecutive y positions (coalesced)
-      float2* gk = rp.Sk + poff + (size_t)k2 * NY + yp;
+      float2* gk = rp.Sk + poff + it;  // it == k2 NY + yp
       constexpr size_t SK1 = (size_t)N2z * NY;  // stride of k1
       float2 d[N1z], u[N1z];
       if (MODE != YZ_IMPORT) {
@@ -1044,50 +1097,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
       for (int k1 = 0; k1 < N1z; ++k1) d[k1] = pc[k1 * PY];
       Dft<N1z>::fwd(d);
 #pragma unroll
-      for (int k1 = 0; k1 < N1z; ++k1) {
-        const int kz = k2 + N2z * k1;
-        const float2 dd = make_float2(d[k1].x * inv_nyz, d[k1].y * inv_nyz);  // normalised D_hat
-        if (MODE == YZ_IMPORT) {
-          u[k1] = dd;
-          continue;
-        }
-        const float2 uu = u[k1];
-        const float q2 = qx2 + qy2 + __ldg(sh.qz2 + kz);
-        const float qn_z = __ldg(sh.qnz + kz);
-        if (MODE == YZ_MAIN) {
-          const float kn2 = qnx * qnx + qn_y * qn_y + qn_z * qn_z;
-          fint = fmaf(kn2, uu.x * uu.x + uu.y * uu.y, fint);
-          if (!is_c) {
-            // AC (:1015-1024): u += (-L dt kappa q^2 u - L dt D) / (1 + L kappa dt q^2)
-            const float lk = rp.L * rp.dt;
-            const float inv = 1.0f / fmaf(lk * rp.kappa_phi, q2, 1.0f);
-            const float m1 = -lk * rp.kappa_phi * q2 * inv;
-            const float m2 = -lk * inv;
-            u[k1] = make_float2(uu.x + fmaf(m1, uu.x, m2 * dd.x), uu.y + fmaf(m1, uu.y, m2 * dd.y));
-          } else {
-            // CH (:976-983): c += (-D dt kappa_c K4 c + D K2 dt mu) / (1 + D dt kappa_c K4), K2 = -q^2
-            const float q4 = qx4 + qy4 + __ldg(sh.qz4 + kz);
-            const float dm = rp.D_L * rp.dt;
-            const float inv = 1.0f / fmaf(dm * rp.kappa_c, q4, 1.0f);
-            const float m1 = -dm * rp.kappa_c * q4 * inv;
-            const float m2 = -dm * q2 * inv;
-            u[k1] = make_float2(uu.x + fmaf(m1, uu.x, m2 * dd.x), uu.y + fmaf(m1, uu.y, m2 * dd.y));
-            if (var_c) {
-              // J_hat = G mu_hat - kappa_c c_hat K3 (:932-935), G = i g, K3 = i k3
-              const float g = qnx + qn_y + qn_z;
-              const float k3 = -(qnx * qx2 + qn_y * qy2 + qn_z * __ldg(sh.qz2 + kz));
-              d[k1] = cmul_pi(make_float2(g * dd.x - rp.kappa_c * k3 * uu.x, g * dd.y - rp.kappa_c * k3 * uu.y));
-            }
-          }
-        } else {
-          // C2: c += dt G J'_hat / (1 + D dt kappa_c K4)  (:976)
-          const float q4 = qx4 + qy4 + __ldg(sh.qz4 + kz);
-          const float dm = rp.D_L * rp.dt;
-          const float g = qnx + qn_y + qn_z;
-          const float sgl = rp.dt * g / fmaf(dm * rp.kappa_c, q4, 1.0f);
-          u[k1] = cadd(uu, cmul_pi(make_float2(dd.x * sgl, dd.y * sgl)));
-        }
-      }
+      for (int k1 = 0; k1 < N1z; ++k1) kpoint<MODE>(P, R, qzt[k2 + N2z * k1], is_c, var_c, u[k1], d[k1], fint);
 #pragma unroll
       for (int k1 = 0; k1 < N1z; ++k1) gk[k1 * SK1] = u[k1];
       if (MODE != YZ_IMPORT) {
@@ -1141,7 +1151,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   }
 
   if (MODE == YZ_MAIN) {
-    double v = warp_sum((double)fint);
+    const double v = (double)warp_sumf(fint);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) red[wid] = v;
     __syncthreads();
