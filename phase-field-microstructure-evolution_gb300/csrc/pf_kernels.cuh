@@ -1049,7 +1049,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
 #pragma unroll
     for (int k2 = 1; k2 < N2y; ++k2) wt[k2] = __ldg(sh.twY + n1 * k2);
     constexpr int ITEMS = NZ * N1y, ITER = (ITEMS + T - 1) / T;
-#pragma unroll 2
+#pragma unroll 4
     for (int j = 0; j < ITER; ++j) {
       const int it = threadIdx.x + j * T;
       if (ITEMS % T != 0 && it >= ITEMS) break;
@@ -1129,7 +1129,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
 #pragma unroll
     for (int k2 = 1; k2 < N2y; ++k2) wt[k2] = __ldg(sh.twY + n1 * k2);
     constexpr int ITEMS = NZ * N1y, ITER = (ITEMS + T - 1) / T;
-#pragma unroll 2
+#pragma unroll 4
     for (int j = 0; j < ITER; ++j) {
       const int it = threadIdx.x + j * T;
       if (ITEMS % T != 0 && it >= ITEMS) break;
