@@ -580,11 +580,13 @@ enum YZMode { YZ_MAIN = 0, YZ_C2 = 1, YZ_IMPORT = 2 };
 // The reference's forms (var_diff.f90 lines cited at the call sites)
 //   AC: u += (-L dt kappa q^2 u - L dt D) / (1 + L dt kappa q^2)
 //   CH: c += (-D dt kappa_c K4 c - D dt q^2 mu) / (1 + D dt kappa_c K4)
-// are evaluated in the algebraically equal folded form u' = (u - b D) /
-// (1 + a Q), Q = q^2 (AC) or K4 (CH), with the 1/(NY NZ) normalisation of the
-// transform folded into b, and the single-precision fast reciprocal (about
-// 2 ulp, far below the step's own FP32 rounding).  The kz factors come from a
-// shared-memory table {qz^2, qz^4, qn_z, qn_z^2} staged once per CTA.
+// are evaluated as u' = u - (t u + b D) / (1 + t), t = a Q, Q = q^2 (AC) or
+// K4 (CH), with the 1/(NY NZ) normalisation of the transform folded into b.
+// The increment is formed first and added to u, as in the reference: the
+// rounding of the (fast, about 2 ulp) reciprocal then scales only the
+// increment, so low modes, whose factor is close to 1, do not drift by a
+// fixed relative bias per step.  The kz factors come from a shared-memory
+// table {qz^2, qz^4, qn_z, qn_z^2} staged once per CTA.
 // ---------------------------------------------------------------------------
 template <int NZ, int T>
 __device__ __forceinline__ void stage_kz(float4* qt, const Shape& sh) {
@@ -596,7 +598,7 @@ __device__ __forceinline__ void stage_kz(float4* qt, const Shape& sh) {
 
 struct KPlane {
   float qx2, qx4, qnx;
-  float a;    // slope of the denominator in Q
+  float a;    // t = a Q
   float b;    // coefficient of the driving term, normalisation included
   float nrm;  // 1 / (NY NZ)
   float kc;   // kappa_c
@@ -646,13 +648,17 @@ __device__ __forceinline__ void kpoint(const KPlane& P, const KRow& R, const flo
     fint = fmaf(R.n2 + z.w, fmaf(uu.x, uu.x, uu.y * uu.y), fint);
     if (!is_c) {
       // AC (:1015-1024)
-      const float inv = __fdividef(1.0f, fmaf(P.a, q2, 1.0f));
-      u = make_float2(fmaf(-P.b, d.x, uu.x) * inv, fmaf(-P.b, d.y, uu.y) * inv);
+      const float t = P.a * q2;
+      const float inv = __fdividef(1.0f, 1.0f + t);
+      const float ix = fmaf(t, uu.x, P.b * d.x), iy = fmaf(t, uu.y, P.b * d.y);
+      u = make_float2(fmaf(-ix, inv, uu.x), fmaf(-iy, inv, uu.y));
     } else {
       // CH (:976-983), K2 = -q^2
-      const float inv = __fdividef(1.0f, fmaf(P.a, R.q4 + z.y, 1.0f));
+      const float t = P.a * (R.q4 + z.y);
+      const float inv = __fdividef(1.0f, 1.0f + t);
       const float bq = P.b * q2;
-      u = make_float2(fmaf(-bq, d.x, uu.x) * inv, fmaf(-bq, d.y, uu.y) * inv);
+      const float ix = fmaf(t, uu.x, bq * d.x), iy = fmaf(t, uu.y, bq * d.y);
+      u = make_float2(fmaf(-ix, inv, uu.x), fmaf(-iy, inv, uu.y));
       if (var_c) {
         // J_hat = G mu_hat - kappa_c c_hat K3 (:932-935), G = i g, K3 = -i (qn . q^2)
         const float gn = (R.g + z.z) * P.nrm;
