@@ -87,9 +87,10 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-// FP32 warp sum: the per-warp partials of the diagnostics (32 FP32 thread
-// sums) are then added in FP64 per block and across blocks; FP64 arithmetic
-// is scarce on this part, FP32 shuffles are not.
+// FP32 warp sum for the yz pass's f_int partials (32 FP32 thread sums); the
+// per-warp results are added in FP64 per block and across blocks.  FP64
+// arithmetic is scarce on this part, FP32 shuffles are not.  (The x pass keeps
+// FP64 shuffles for its partials: with FP32 ones that kernel measured slower.)
 __device__ __forceinline__ float warp_sumf(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
