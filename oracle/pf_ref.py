@@ -387,19 +387,26 @@ def ic_plane(p: Params, ppt_rad, i_ppt: int, j_ppt: int, k_ppt: int, c_mat: floa
     return phi, con
 
 
-def insert_precipitates(p: Params, phi: np.ndarray, ppt_rad, num_ppt: int, idum: int, gen: "Ran2"):
+def insert_precipitates(p: Params, phi: np.ndarray, ppt_rad, num_ppt: int, idum: int, gen: "Ran2",
+                        max_attempts: int = 10 ** 8):
     """Precipitates added at step ``ppt_int``, ``src/var_diff.f90:479-554``
     (one rank).  A ran_2 position is rejected while the matrix variants there
     have sum phi_i^2 > 0.8 (inside a grain) or any cell of the sphere already
     has phi_var > 0; an accepted sphere gets phi_var = 1 and the matrix
     variants 0 (con is left as it is).  Modifies phi in place; returns
-    idum_after."""
+    idum_after.  The reference loops until it succeeds; here more than
+    ``max_attempts`` draws raise RuntimeError (the library gives up after
+    1e8 with PF_EINVAL)."""
     var = p.var
     rad_ppt = ppt_rad[0] ** 2 + ppt_rad[1] ** 2 + ppt_rad[2] ** 2
     zz, yy, xx = np.meshgrid(np.arange(1, p.Nz + 1), np.arange(1, p.Ny + 1),
                              np.arange(1, p.Nx + 1), indexing="ij")
     nppt = 1
+    attempts = 0
     while nppt <= num_ppt:
+        attempts += 1
+        if attempts > max_attempts:
+            raise RuntimeError("precipitate insertion: no admissible place")
         r, idum = gen(idum)
         ix = int(r * p.Nx + 1.0)
         r, idum = gen(idum)

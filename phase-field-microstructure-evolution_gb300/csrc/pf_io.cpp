@@ -6,6 +6,7 @@
 //  * the reference's 'circle', 'plane' and 'polycryst' starts
 //    (src/var_diff.f90:229-449) and the precipitate insertion at ppt_int
 //    (:479-554), all on one rank (ist = 1, ien = N).
+#include <algorithm>
 #include <cctype>
 #include <cerrno>
 #include <cmath>
@@ -172,6 +173,41 @@ bool in_ellipsoid(int i, int j, int k, int rx, int ry, int rz) {
   return s <= 1.0;
 }
 
+// The cells (i, j, k) with (i-ix)^2 + (j-jy)^2 + (k-kz)^2 <= rad, no periodic
+// wrap, that the reference's precipitate placement finds by scanning the
+// whole grid (src/var_diff.f90:424-447, :517-548).  Only the bounding box of
+// that ball, clipped to the grid, can hold one, so both scans visit that box:
+// the same cells in the same order, O(R^3) per attempt instead of O(N^3).
+struct Ball {
+  int ix, jy, kz, rad, i0, i1, j0, j1, k0, k1;
+  Ball(const pf_config* c, int x, int y, int z, int r2) : ix(x), jy(y), kz(z), rad(r2) {
+    int R = 0;  // largest offset with R^2 <= rad
+    while ((R + 1) * (R + 1) <= rad) ++R;
+    i0 = std::max(1, ix - R); i1 = std::min(c->nx, ix + R);
+    j0 = std::max(1, jy - R); j1 = std::min(c->ny, jy + R);
+    k0 = std::max(1, kz - R); k1 = std::min(c->nz, kz + R);
+  }
+  bool inside(int i, int j, int k) const {
+    return (i - ix) * (i - ix) + (j - jy) * (j - jy) + (k - kz) * (k - kz) <= rad;
+  }
+  // does any cell of the ball already have phi_V > 0?
+  bool hits(const pf_config* c, const double* phi) const {
+    const int V = c->var;
+    for (int k = k0; k <= k1; ++k)
+      for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i)
+          if (inside(i, j, k) && phi[cell(c, i, j, k) * V + (V - 1)] > 0.0) return true;
+    return false;
+  }
+  template <class F>
+  void each(F f) const {
+    for (int k = k0; k <= k1; ++k)
+      for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i)
+          if (inside(i, j, k)) f(i, j, k);
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -323,23 +359,13 @@ int pf_ic_circle(const pf_config* c, int grn_rad, const int* ppt_rad, int num_pp
     const int ix = (int)(pf_ran2(st, idum) * Nx + 1.0);
     const int jy = (int)(pf_ran2(st, idum) * Ny + 1.0);
     const int kz = (int)(pf_ran2(st, idum) * Nz + 1.0);
-    bool hit = false;
-    for (int k = 1; k <= Nz && !hit; ++k)
-      for (int j = 1; j <= Ny && !hit; ++j)
-        for (int i = 1; i <= Nx; ++i) {
-          const int d = (i - ix) * (i - ix) + (j - jy) * (j - jy) + (k - kz) * (k - kz);
-          if (d <= rad && phi[cell(c, i, j, k) * V + (V - 1)] > 0.0) { hit = true; break; }
-        }
-    if (hit) continue;
-    for (int k = 1; k <= Nz; ++k)
-      for (int j = 1; j <= Ny; ++j)
-        for (int i = 1; i <= Nx; ++i) {
-          const int d = (i - ix) * (i - ix) + (j - jy) * (j - jy) + (k - kz) * (k - kz);
-          if (d > rad) continue;
-          double* p = phi + cell(c, i, j, k) * V;
-          p[2] = 1.0; p[1] = 0.0; p[0] = 0.0;
-          con[cell(c, i, j, k)] = con_0_ppt;
-        }
+    const Ball ball(c, ix, jy, kz, rad);
+    if (ball.hits(c, phi)) continue;
+    ball.each([&](int i, int j, int k) {
+      double* p = phi + cell(c, i, j, k) * V;
+      p[2] = 1.0; p[1] = 0.0; p[0] = 0.0;
+      con[cell(c, i, j, k)] = con_0_ppt;
+    });
     ++nppt;
   }
   return PF_OK;
@@ -419,23 +445,13 @@ int pf_insert_precipitates(const pf_config* c, const int* ppt_rad, int num_ppt, 
         s += fi * fi;
       }
     if (s > 0.8) continue;  // inside a grain: try again
-    bool hit = false;
-    for (int k = 1; k <= Nz && !hit; ++k)
-      for (int j = 1; j <= Ny && !hit; ++j)
-        for (int i = 1; i <= Nx; ++i) {
-          const int d = (i - ix) * (i - ix) + (j - jy) * (j - jy) + (k - kz) * (k - kz);
-          if (d <= rad && phi[cell(c, i, j, k) * V + (V - 1)] > 0.0) { hit = true; break; }
-        }
-    if (hit) continue;
-    for (int k = 1; k <= Nz; ++k)
-      for (int j = 1; j <= Ny; ++j)
-        for (int i = 1; i <= Nx; ++i) {
-          const int d = (i - ix) * (i - ix) + (j - jy) * (j - jy) + (k - kz) * (k - kz);
-          if (d > rad) continue;
-          double* p = phi + cell(c, i, j, k) * V;
-          p[V - 1] = 1.0;
-          for (int f = 0; f < mat; ++f) p[f] = 0.0;
-        }
+    const Ball ball(c, ix, jy, kz, rad);
+    if (ball.hits(c, phi)) continue;
+    ball.each([&](int i, int j, int k) {
+      double* p = phi + cell(c, i, j, k) * V;
+      p[V - 1] = 1.0;
+      for (int f = 0; f < mat; ++f) p[f] = 0.0;
+    });
     ++nppt;
   }
   return PF_OK;

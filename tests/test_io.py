@@ -290,6 +290,34 @@ def test_insert_precipitates_matches_oracle(pkg, oracle):
     assert np.count_nonzero(phi[-1] == 1.0) >= 5
 
 
+@pytest.mark.parametrize("rad,num", [((4, 3, 5), 3), ((1, 1, 1), 6), ((6, 6, 6), 1)])
+def test_insert_precipitates_large_balls_at_the_edges(pkg, oracle, rad, num):
+    """Balls larger than the margin to the grid's faces (the reference does
+    not wrap them) and a non-cubic grid: same cells and ran_2 stream as the
+    oracle's whole-grid scan."""
+    p = oracle.Params(Nx=24, Ny=20, Nz=28, var=4)
+    phi0, _ = oracle.ic_voronoi(p, 5, 5, 0.0, 0.5, 0.0)
+    phi0 = phi0 * 0.6
+    phi0[-1] = 0.0  # no precipitate phase yet: every position outside the balls is free
+    gen = oracle.Ran2()
+    phi_o = phi0.copy()
+    idum_o = oracle.insert_precipitates(p, phi_o, rad, num, -3, gen, max_attempts=20000)
+    rng = pkg.Ran2(-3)
+    phi = pkg.insert_precipitates(p, phi0, rad, num, rng)
+    assert np.array_equal(phi, phi_o)
+    assert rng.idum.value == idum_o
+    assert np.count_nonzero(phi[-1] == 1.0) > 0
+
+
+def test_ic_circle_edge_balls_match_oracle(pkg, oracle):
+    p = oracle.Params(Nx=20, Ny=24, Nz=16, var=3)
+    gen = oracle.Ran2()
+    phi_o, con_o, idum_o = oracle.ic_circle(p, 5, (3, 2, 4), 2, -9, 0.3, 0.7, gen=gen)
+    phi, con, rng = pkg.ic_circle(p, 5, (3, 2, 4), 2, -9, 0.3, 0.7)
+    assert np.array_equal(phi, phi_o) and np.array_equal(con, con_o)
+    assert rng.idum.value == idum_o
+
+
 def test_driver_writes_headers(pkg, oracle, tmp_path):
     """Without a GPU the driver writes its headers and gamma_matrix.dat, then
     stops at pf_create with status 2; with one it runs to the end."""
