@@ -10,6 +10,11 @@ step of that run; the metric is cell-steps/s x P = Nx Ny Nz * P * steps / s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+--workload large times the 256^3 grid with 32 order parameters instead (256
+grains from seed 2, c = 0.4 + U(-0.02, 0.02), kappa = 2, constant mobility,
+dt = 0.1; 5000 steps for the full run), with the same line; --var overrides
+the number of order parameters of either grid (small profiling cases).
+
 Under torchrun (N > 1) every rank steps its own independent replica (seed
 1 + rank) on its own GPU; there is no data-path collective ("replicas only").
 """
@@ -32,6 +37,8 @@ WORKLOAD = dict(Nx=128, Ny=128, Nz=128, var=16, t_step=0.1, grad_coeff_phi=1.0, 
                 mobility="c1mc")
 IC = dict(seed=1, n_grains=64, amp_phi=0.01, c0=0.5, amp_c=0.02)
 WORKLOAD_NAME = "polycrystal 128^3, P=16, M(c)=M0(1+c(1-c)), 64 Voronoi grains seed 1, dt=0.1"
+TRAFFIC_SUFFIX = ""  # key suffix of the ncu traffic figures for a non-headline workload
+_HEADLINE = (dict(WORKLOAD), dict(IC), WORKLOAD_NAME)
 METRIC = "cell-steps/s x P"
 FALLBACK_HBM_GBS = 6800.0
 
@@ -40,6 +47,23 @@ def params(**over):
     d = dict(WORKLOAD)
     d.update(over)
     return SimpleNamespace(**d)
+
+
+def select_workload(name: str, var: int | None = None) -> None:
+    """Point WORKLOAD / IC / WORKLOAD_NAME at the polycrystal headline grid
+    or the large grid, optionally with another number of order parameters."""
+    global WORKLOAD, IC, WORKLOAD_NAME, TRAFFIC_SUFFIX
+    WORKLOAD, IC, WORKLOAD_NAME, TRAFFIC_SUFFIX = dict(_HEADLINE[0]), dict(_HEADLINE[1]), _HEADLINE[2], ""
+    if name == "large":
+        WORKLOAD = dict(WORKLOAD, Nx=256, Ny=256, Nz=256, var=32, grad_coeff_phi=2.0, grad_coeff_c=2.0,
+                        mobility="reference", D_gb=0.0)
+        IC = dict(seed=2, n_grains=256, amp_phi=0.01, c0=0.4, amp_c=0.02)
+        WORKLOAD_NAME = "polycrystal 256^3, P=32, constant mobility, 256 Voronoi grains seed 2, c0=0.4, kappa=2, dt=0.1"
+    if var is not None and var != WORKLOAD["var"]:
+        WORKLOAD = dict(WORKLOAD, var=var)
+        WORKLOAD_NAME = f"{WORKLOAD_NAME} [P={var} by --var]"
+    if name != "polycrystal" or var is not None:
+        TRAFFIC_SUFFIX = f"@{WORKLOAD['Nx']}^3xP{WORKLOAD['var']}"
 
 
 # ---------------------------------------------------------------------------
@@ -313,7 +337,7 @@ def run_ours(args):
     dom = kernels[dom_name]
     peak, peak_kind = measured_hbm()
     achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
-    traffic = ncu_traffic(dom_name)
+    traffic = ncu_traffic(dom_name + TRAFFIC_SUFFIX)
 
     # end to end through the C ABI with host buffers: upload the start fields
     # from pinned memory, K steps with their diagnostic records returned to the
@@ -386,7 +410,11 @@ def run_ours(args):
             v64 = cells * p.var * n64 / t64
             line["fp64_gpu_path"] = {"value": v64, "unit": METRIC, "steps": n64,
                                      "ratio": value / v64, "what": "PF_FP64_PLAIN, host wall clock per pf_step call"}
-        if not args.no_cpu_baseline and ws == 1:
+        if not args.no_cpu_baseline and ws == 1 and p.Nx * p.Ny * p.Nz * p.var > (128 ** 3) * 16:
+            # one FP64 CPU step of a grid this size takes minutes on the host cores
+            line["cpu_baseline"] = {"value": None, "skipped": "one FP64 step of this grid on the CPU restatement "
+                                                              "takes about two minutes on 16 cores"}
+        elif not args.no_cpu_baseline and ws == 1:
             v, cores, sample, n, dt, _ = cpu_port_throughput(p, 20.0, 50)
             line["cpu_baseline"] = {"value": v, "unit": "cell-steps/s x P", "cores": cores, "kind": "port",
                                     "sample": sample}
@@ -581,8 +609,11 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU path comparison")
-    ap.add_argument("--workload", choices=["polycrystal", "ensemble", "serve"], default="polycrystal",
-                    help="polycrystal (the headline line), ensemble (config 3) or serve (config 4)")
+    ap.add_argument("--workload", choices=["polycrystal", "large", "ensemble", "serve"], default="polycrystal",
+                    help="polycrystal (the headline line, 128^3 x 16), large (256^3 x 32), ensemble (config 3) "
+                         "or serve (config 4)")
+    ap.add_argument("--var", type=int, default=None,
+                    help="polycrystal / large: another number of order parameters (small profiling cases)")
     ap.add_argument("--runs", type=int, default=256, help="ensemble: runs in the batch")
     ap.add_argument("--requests", type=int, default=24, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=8.0, help="serve: Poisson arrival rate (requests/s)")
@@ -590,6 +621,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.workload in ("polycrystal", "large"):
+        select_workload(args.workload, args.var)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "ensemble":

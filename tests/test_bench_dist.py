@@ -53,3 +53,26 @@ def test_reference_arm_runs_on_rank_0_only():
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "3"], capture_output=True, text=True, timeout=120, env=env)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_large_workload_selection():
+    """--workload large is the 256^3 x 32 polycrystal (256 grains, seed 2,
+    c0 = 0.4, kappa = 2, constant mobility); --var changes only P and keys the
+    ncu traffic figure by grid and P.  Run in a child process: the selection
+    sets module globals."""
+    code = ("import sys; sys.path.insert(0, %r); import bench\n"
+            "bench.select_workload('large'); p = bench.params()\n"
+            "assert (p.Nx, p.Ny, p.Nz, p.var, p.mobility, p.D_gb) == (256, 256, 256, 32, 'reference', 0.0)\n"
+            "assert (p.grad_coeff_phi, p.grad_coeff_c, p.t_step) == (2.0, 2.0, 0.1)\n"
+            "assert bench.IC == dict(seed=2, n_grains=256, amp_phi=0.01, c0=0.4, amp_c=0.02)\n"
+            "assert bench.TRAFFIC_SUFFIX == '@256^3xP32' and bench.replica_seed(1) == 3\n"
+            "bench.select_workload('polycrystal', 4)\n"
+            "assert bench.params().Nx == 128 and bench.params().var == 4 and bench.TRAFFIC_SUFFIX == '@128^3xP4'\n"
+            "bench.select_workload('large', 4)\n"
+            "assert bench.params().Nx == 256 and bench.params().var == 4 and bench.TRAFFIC_SUFFIX == '@256^3xP4'\n"
+            ) % str(ROOT)
+    subprocess.run([sys.executable, "-c", code], check=True, timeout=120)
+    code = ("import sys; sys.path.insert(0, %r); import bench\n"
+            "bench.select_workload('polycrystal'); p = bench.params()\n"
+            "assert (p.Nx, p.var, p.mobility) == (128, 16, 'c1mc') and bench.TRAFFIC_SUFFIX == ''\n") % str(ROOT)
+    subprocess.run([sys.executable, "-c", code], check=True, timeout=120)
