@@ -992,16 +992,22 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
 // y positions, so column accesses are conflict-free).  No re-layout, no
 // cluster.  Same k-space position order as the cluster kernel.
 // ---------------------------------------------------------------------------
-template <int NY, int NZ>
+// Row pitch: the odd line pitch, or (RAWP) the unpadded run layout
+// N2 (N1 + 1).  yz1 reads columns with lanes along y, so only its row passes
+// see the pitch: a warp covers two rows (first/last y pass) or 32/N2 rows of
+// N2 runs (pass B); with N2 (N1 + 1) = 8 (mod 16) float2 the rows of a half
+// warp fall in disjoint bank pairs (128 x 128: no conflicts, against one
+// extra wavefront in four at the odd pitch).
+template <int NY, int NZ, bool RAWP = false>
 struct YZ1 {
-  static constexpr int PY = Line<NY>::PITCH;
+  static constexpr int PY = RAWP ? Line<NY>::RAW : Line<NY>::PITCH;
   static constexpr size_t SMEM = (size_t)NZ * PY * sizeof(float2);
 };
 
 // column pass A (forward or inverse) over the NY y positions
-template <int NY, int NZ, int T, bool INV>
+template <int NY, int NZ, int T, bool INV, bool RAWP>
 __device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
-  constexpr int N1 = Line<NZ>::N1, N2 = Line<NZ>::N2, PY = YZ1<NY, NZ>::PY;
+  constexpr int N1 = Line<NZ>::N1, N2 = Line<NZ>::N2, PY = YZ1<NY, NZ, RAWP>::PY;
   constexpr int ITEMS = NY * N1, ITER = (ITEMS + T - 1) / T;
 #pragma unroll 1
   for (int j = 0; j < ITER; ++j) {
@@ -1027,12 +1033,12 @@ __device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
   }
 }
 
-template <int NY, int NZ, int T, int MODE>
+template <int NY, int NZ, int T, int MODE, bool RAWP = false>
 __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using LY = Line<NY>;
   using LZ = Line<NZ>;
   constexpr int N1y = LY::N1, N2y = LY::N2, N1z = LZ::N1, N2z = LZ::N2;
-  constexpr int PY = YZ1<NY, NZ>::PY;
+  constexpr int PY = YZ1<NY, NZ, RAWP>::PY;
   static_assert(T % N1y == 0 && T % N2y == 0, "thread count");
   extern __shared__ float2 U[];
   __shared__ double red[T / 32];
@@ -1075,7 +1081,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   __syncthreads();
   passB<NY, NZ, PY, T, false>(U);
   __syncthreads();
-  colA<NY, NZ, T, false>(U, sh.twZ);
+  colA<NY, NZ, T, false, RAWP>(U, sh.twZ);
   __syncthreads();
 
   // 2. last forward z pass, pointwise k-space update, first inverse z pass
@@ -1122,7 +1128,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   }
   if (MODE == YZ_IMPORT) return;
   __syncthreads();
-  colA<NY, NZ, T, true>(U, sh.twZ);
+  colA<NY, NZ, T, true, RAWP>(U, sh.twZ);
   __syncthreads();
   passB<NY, NZ, PY, T, true>(U);
   __syncthreads();

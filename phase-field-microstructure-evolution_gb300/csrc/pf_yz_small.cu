@@ -17,16 +17,16 @@ static int add(YZKernels* out, int n) {
   return n + 1;
 }
 
-template <int NY, int NZ, int T>
+template <int NY, int NZ, int T, bool RAWP = false>
 static int add1(YZKernels* out, int n) {
   if (n >= kMaxVariants) return n;
   YZKernels& k = out[n];
-  k.main = yz1_kernel<NY, NZ, T, YZ_MAIN>;
-  k.c2 = yz1_kernel<NY, NZ, T, YZ_C2>;
-  k.imp = yz1_kernel<NY, NZ, T, YZ_IMPORT>;
+  k.main = yz1_kernel<NY, NZ, T, YZ_MAIN, RAWP>;
+  k.c2 = yz1_kernel<NY, NZ, T, YZ_C2, RAWP>;
+  k.imp = yz1_kernel<NY, NZ, T, YZ_IMPORT, RAWP>;
   k.cluster = 1;
   k.threads = T;
-  k.smem = YZ1<NY, NZ>::SMEM;
+  k.smem = YZ1<NY, NZ, RAWP>::SMEM;
   return n + 1;
 }
 
@@ -46,11 +46,13 @@ int yz_variants_small(int ny, int nz, YZKernels* out, int n) {
     n = add1<64, 64, 128>(out, n);
     n = add1<64, 64, 512>(out, n);
     n = add<64, 64, 2, 256>(out, n);
+    n = add1<64, 64, 256, true>(out, n);  // unpadded row pitch
   }
   if (ny == 96 && nz == 96) {  // the reference's own grid (inputs/config.yaml, inputs/input.txt)
     n = add1<96, 96, 384>(out, n);
     n = add1<96, 96, 192>(out, n);
     n = add1<96, 96, 768>(out, n);
+    n = add1<96, 96, 384, true>(out, n);  // unpadded row pitch
   }
   return n;
 }
