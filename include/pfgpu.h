@@ -134,7 +134,9 @@ typedef struct pf_server_config {
   int device;
   int max_active;          /* runs resident at once (0: 64) */
   double hbm_budget_bytes; /* device memory the server's runs may hold (0: 80 % of free memory at create) */
-  int chunk_steps;         /* steps a batch is given at a time (0: 128, at most 1024) */
+  int chunk_steps;         /* steps a batch is given at a time (0: 128; larger values are cut to 512,
+                              so that the records of the two chunks kept in flight fit the per-run
+                              ring of 1024 records) */
   int reserved[5];
 } pf_server_config;
 typedef struct pf_request_times {
@@ -203,12 +205,14 @@ double pf_ran2(pf_ran2_state* st, int* idum);
  * already holds on the current device, with no allocation.
  *   fields: float [var+1][nz][ny][nx] device memory, phi_1..phi_var then c;
  *   out:    host record; f_int and e_tot are NaN (they need the transforms);
- *   stream: cudaStream_t or NULL; the call waits for its own work.
+ *           nonfinite counts the cells holding a NaN or Inf value;
+ *   stream: cudaStream_t or NULL; the call waits for its own work, so it is
+ *           rejected (PF_EINVAL) on a stream that is being captured.
  * Scratch is a fixed 512 KiB __device__ array present on every GPU that loads
  * the library until the process exits; grids above PF_NOALLOC_MAX_CELLS are
- * rejected with PF_EINVAL.  The first call on a device looks up the scratch
- * address there: make it before any stream capture.  All calls share the
- * scratch, so calls that overlap on the GPU race. */
+ * rejected with PF_EINVAL.  Every call looks the array up in the current
+ * context.  All calls share the scratch, so calls that overlap on the GPU
+ * race. */
 #define PF_NOALLOC_MAX_CELLS (256 * 256 * 256)
 int pf_diag_fields_noalloc(const pf_config* cfg, const float* fields, pf_diag* out, void* stream);
 

@@ -433,6 +433,38 @@ def insert_precipitates(p: Params, phi: np.ndarray, ppt_rad, num_ppt: int, idum:
 # ---------------------------------------------------------------------------
 # One time step: src/var_diff.f90:556-1050 and the statistics at :1076-1118
 # ---------------------------------------------------------------------------
+def bulk_energies(p: Params, phi: np.ndarray, con: np.ndarray, gamma=None, dtype=np.float64):
+    """Phases 5-6 of one step from the fields at its start:
+    f_eta (``src/var_diff.f90:685-719``), h = phi_mat = N4/S4, f_ch and df_dc
+    (``:723-757``).  Returns (f_eta, f_ch, phi_mat, S4, df_dc); an all-zero
+    cell gives phi_mat = 0/0 = NaN, as in the reference."""
+    var = p.var
+    P = var - 1
+    g = gamma_matrix(var, p.sigma_1, p.sigma_2) if gamma is None else gamma
+    f_eta_c = np.zeros(p.shape, dtype=dtype)
+    for i in range(var):
+        fi2 = phi[i] * phi[i]
+        f_eta_c += -0.5 * fi2 + 0.25 * fi2 * fi2
+        for j in range(i + 1, var):
+            f_eta_c += g[i, j] * fi2 * (phi[j] * phi[j])
+    f_eta = float(np.sum(f_eta_c))
+    num = np.zeros(p.shape, dtype=dtype)
+    den = np.zeros(p.shape, dtype=dtype)
+    for i in range(var):
+        f4 = phi[i] ** 4
+        if i < P:
+            num += f4
+        den += f4
+    with np.errstate(invalid="ignore", divide="ignore"):
+        phi_mat = num / den
+    phi_ppt = 1.0 - phi_mat
+    dcm = con - p.con_0_mat
+    dcp = con - p.con_0_ppt
+    f_ch = float(np.sum(phi_mat * p.am * dcm ** 2 + phi_ppt * p.ap * dcp ** 2))
+    df_dc = 2.0 * phi_mat * p.am * dcm + 2.0 * phi_ppt * p.ap * dcp
+    return f_eta, f_ch, phi_mat, den, df_dc
+
+
 @dataclasses.dataclass
 class Diag:
     """Per-step diagnostics.  f_int, f_eta, f_ch use the fields at the START
@@ -528,30 +560,9 @@ class Oracle:
 
         f_int = self._f_int()
 
-        # phase 5: f_eta (src/var_diff.f90:685-719)
-        f_eta_c = np.zeros(p.shape, dtype=self.dtype)
-        for i in range(var):
-            fi2 = phi[i] * phi[i]
-            f_eta_c += -0.5 * fi2 + 0.25 * fi2 * fi2
-            for j in range(i + 1, var):
-                f_eta_c += g[i, j] * fi2 * (phi[j] * phi[j])
-        f_eta = float(np.sum(f_eta_c))
-
-        # phase 6: h, f_ch, df_dc (src/var_diff.f90:723-757)
-        num = np.zeros(p.shape, dtype=self.dtype)
-        den = np.zeros(p.shape, dtype=self.dtype)
-        for i in range(var):
-            f4 = phi[i] ** 4
-            if i < P:
-                num += f4
-            den += f4
-        with np.errstate(invalid="ignore", divide="ignore"):
-            phi_mat = num / den
-        phi_ppt = 1.0 - phi_mat
+        f_eta, f_ch, phi_mat, den, df_dc = bulk_energies(p, phi, con, g, self.dtype)
         dcm = con - p.con_0_mat
         dcp = con - p.con_0_ppt
-        f_ch = float(np.sum(phi_mat * p.am * dcm ** 2 + phi_ppt * p.ap * dcp ** 2))
-        df_dc = 2.0 * phi_mat * p.am * dcm + 2.0 * phi_ppt * p.ap * dcp
 
         # phase 7: term1, term2 (src/var_diff.f90:767-803)
         df_dphi = np.empty_like(phi)

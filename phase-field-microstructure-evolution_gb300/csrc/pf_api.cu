@@ -42,66 +42,6 @@ static int fail(int code, const char* fmt, ...) {
                                        __FILE__, __LINE__);                                      \
   } while (0)
 
-// ---------------------------------------------------------------------------
-// Per-step reduction of block partials into one diagnostic record.
-// One block per run, fixed summation order: results do not depend on how many
-// other runs share the launch.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) reduce_diag_kernel(const RunParams* __restrict__ runs, const Shape sh) {
-  const RunParams& rp = runs[blockIdx.x];
-  constexpr int NT = 1024;
-  __shared__ double sd[5][NT / 32];
-  __shared__ float sf[4][NT / 32];
-  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  double a_eta = 0, a_ch = 0, a_mass = 0, a_int = 0, a_bad = 0;
-  float cmin = 1.f, cmax = 0.f, pmin = 1.f, ppmax = 0.f;
-  const int nb = sh.nblk_x;
-  const double* px = rp.part_x;
-#pragma unroll 4
-  for (int i = t; i < nb; i += NT) {
-    a_eta += px[XD_FETA * nb + i];
-    a_ch += px[XD_FCH * nb + i];
-    a_mass += px[XD_MASS * nb + i];
-    cmin = fminf(cmin, (float)px[XD_CMIN * nb + i]);
-    cmax = fmaxf(cmax, (float)px[XD_CMAX * nb + i]);
-    pmin = fminf(pmin, (float)px[XD_PHIMIN * nb + i]);
-    ppmax = fmaxf(ppmax, (float)px[XD_PHIPMAX * nb + i]);
-    a_bad += px[XD_NONFINITE * nb + i];
-  }
-#pragma unroll 4
-  for (int i = t; i < sh.nblk_yz; i += NT) a_int += rp.part_yz[i];
-  a_eta = warp_sum(a_eta); a_ch = warp_sum(a_ch); a_mass = warp_sum(a_mass);
-  a_int = warp_sum(a_int); a_bad = warp_sum(a_bad);
-  cmin = warp_min(cmin); cmax = warp_max(cmax); pmin = warp_min(pmin); ppmax = warp_max(ppmax);
-  if (lane == 0) {
-    sd[0][w] = a_eta; sd[1][w] = a_ch; sd[2][w] = a_mass; sd[3][w] = a_int; sd[4][w] = a_bad;
-    sf[0][w] = cmin; sf[1][w] = cmax; sf[2][w] = pmin; sf[3][w] = ppmax;
-  }
-  __syncthreads();
-  if (t == 0) {
-    double s[5] = {0, 0, 0, 0, 0};
-    float m[4] = {1.f, 0.f, 1.f, 0.f};
-    for (int k = 0; k < NT / 32; ++k) {
-      for (int q = 0; q < 5; ++q) s[q] += sd[q][k];
-      m[0] = fminf(m[0], sf[0][k]); m[1] = fmaxf(m[1], sf[1][k]);
-      m[2] = fminf(m[2], sf[2][k]); m[3] = fmaxf(m[3], sf[3][k]);
-    }
-    const int step = *rp.counter;
-    double* d = rp.diag + (size_t)(step % rp.ring) * DR_COUNT;
-    d[DR_STEP] = step + 1;
-    d[DR_FINT] = s[3];
-    d[DR_FETA] = s[0];
-    d[DR_FCH] = s[1];
-    d[DR_CMIN] = m[0];
-    d[DR_CMAX] = m[1];
-    d[DR_PHIMIN] = m[2];
-    d[DR_PHIPMAX] = m[3];
-    d[DR_MASS] = s[2];
-    d[DR_NONFINITE] = s[4];
-    *rp.counter = step + 1;
-  }
-}
-
 // Fortran-order host fields (REAL*8) <-> float SoA staging [f][z][y][x]
 __global__ void aos_to_soa_kernel(const double* __restrict__ phi, const double* __restrict__ con, float* __restrict__ fin,
                                   int V, size_t ncell) {
@@ -125,7 +65,7 @@ static void twiddles(int L, std::vector<float2>& out) {
   out.resize(L);
   const double pi = std::atan(1.0) * 4.0;
   for (int j = 0; j < L; ++j) {
-    // reduce the angle to the first octant for accuracy, then rebuild
+    // FP64 cos/sin of the angle, rounded once to FP32
     const double a = 2.0 * pi * (double)j / (double)L;
     out[j] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
   }
@@ -255,8 +195,9 @@ struct pf_batch {
   int ring = 0;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t gexec = nullptr;
-  cudaStream_t side = nullptr;        // second branch of the captured step (diagnostics reduction)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_c = nullptr;
+  cudaStream_t side = nullptr;        // second branch of the captured step (concentration chain)
+  cudaStream_t copy = nullptr;        // record copies of completed steps (never waits for later steps)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int prio_hi = 0;                    // greatest stream priority of the device
   std::vector<double> hdiag;
   std::vector<int> steps_done;
@@ -336,14 +277,12 @@ static int launch_x_bulk(pf_batch* b, cudaStream_t s) {
 }
 
 // One step on stream s.  With `branch` (the captured graph) and variable
-// mobility, the concentration field's chain — its yz planes, the xj pass and
-// the yz C2 pass, which the order-parameter planes do not need — runs on a
+// mobility, the concentration field's chain -- its yz planes, the xj pass and
+// the yz C2 pass, which the order-parameter planes do not need -- runs on a
 // second branch at high priority beside the order-parameter planes, so that
-// its small launches fill SMs as the big launch drains; the diagnostics
-// reduction follows the order-parameter planes once the c planes' f_int
-// partials are in.
+// its small launches fill SMs as the big launch drains.  The step's record is
+// formed by whichever yz-pass CTA of a run finishes last (either branch).
 static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
-  const Shape sh = b->tab.sh;
   const int R = b->nruns;
   {
     const int rc0 = launch_x_bulk(b, s);
@@ -356,7 +295,6 @@ static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
     PF_CUDA(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     int rc = launch_yz(b, b->yk.main, b->Kx, b->drp, R, b->side, pc, b->prio_hi);
     if (rc) return rc;
-    PF_CUDA(cudaEventRecord(b->ev_c, b->side));
     rc = launch_xj(b, b->side, b->prio_hi);
     if (rc) return rc;
     rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, b->side, 0, b->prio_hi);
@@ -364,9 +302,6 @@ static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
     PF_CUDA(cudaEventRecord(b->ev_join, b->side));
     rc = launch_yz(b, b->yk.main, pc, b->drp, R, s);
     if (rc) return rc;
-    PF_CUDA(cudaStreamWaitEvent(s, b->ev_c, 0));
-    reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
-    PF_CUDA(cudaGetLastError());
     PF_CUDA(cudaStreamWaitEvent(s, b->ev_join, 0));
     return PF_OK;
   }
@@ -378,8 +313,6 @@ static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
     rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, s);
     if (rc) return rc;
   }
-  reduce_diag_kernel<<<R, 1024, 0, s>>>(b->drp, sh);
-  PF_CUDA(cudaGetLastError());
   return PF_OK;
 }
 
@@ -606,7 +539,7 @@ static int tune_batch(pf_batch* b) {
         PF_CUDA(cudaMemsetAsync(r.Sk, 0, fbytes, b->stream));
         PF_CUDA(cudaMemsetAsync(r.Sm, 0, fbytes, b->stream));
         PF_CUDA(cudaMemsetAsync(r.D, 0, fbytes, b->stream));
-        PF_CUDA(cudaMemsetAsync(r.counter, 0, sizeof(int), b->stream));
+        PF_CUDA(cudaMemsetAsync(r.counter, 0, 128, b->stream));  // step counter and ticket
       }
       PF_CUDA(cudaStreamSynchronize(b->stream));
       g_tune_cache[key] = std::make_tuple(bx, by, bj);
@@ -630,9 +563,9 @@ static void destroy_batch(pf_batch* b) {
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   if (b->stream) cudaStreamDestroy(b->stream);
   if (b->side) cudaStreamDestroy(b->side);
+  if (b->copy) cudaStreamDestroy(b->copy);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   if (b->ev_join) cudaEventDestroy(b->ev_join);
-  if (b->ev_c) cudaEventDestroy(b->ev_c);
   cudaFree(b->drp);
   cudaFree(b->mem);
   cudaFree(b->fin);
@@ -714,6 +647,7 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
     r.part_yz = (double*)p; p += szPyz;
     r.diag = (double*)p; p += szDiag;
     r.counter = (int*)p;
+    r.ticket = (unsigned*)(p + 64);  // own 64-byte line in the 256-byte counter block
     r.fin = b->fin;
     r.L = (float)c.mob_phi;
     r.kappa_phi = (float)c.grad_coeff_phi;
@@ -740,7 +674,7 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   int prio_lo = 0;
   cudaDeviceGetStreamPriorityRange(&prio_lo, &b->prio_hi);
   e = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, b->prio_hi);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_c, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream/events: %s", cudaGetErrorString(e)));
@@ -776,7 +710,7 @@ static int batch_set_fields(pf_batch* b, int run, const double* phi, const doubl
   b->xk.imp<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
   int rc = launch_yz(b, b->yk.imp, b->nF * b->Kx, b->drp + run, 1, b->stream);
   if (rc) return rc;
-  PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, sizeof(int), b->stream));
+  PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, 128, b->stream));  // step counter and ticket
   PF_CUDA(cudaGetLastError());
   PF_CUDA(cudaStreamSynchronize(b->stream));
   b->steps_done[run] = 0;
@@ -978,7 +912,10 @@ int pf_batch_steps_done(pf_batch* b, int run) {
   return (b && run >= 0 && run < b->nruns) ? b->steps_done[run] : -1;
 }
 // Records of steps first .. first+n-1 (0-based, since set_fields) of one run,
-// still in the device ring (n <= the ring length, work complete).
+// still in the device ring (n <= the ring length).  The caller has seen those
+// steps complete (an event recorded after them): the copy runs on the batch's
+// copy stream, so it does not wait for steps enqueued later on the batch's
+// stream, which may go on writing other slots of the ring meanwhile.
 int pf_batch_records(pf_batch* b, int run, int first, int n, pf_diag* out) {
   if (!b || run < 0 || run >= b->nruns || n < 0 || n > b->ring || !out) return fail(PF_EINVAL, "bad arguments");
   PF_CUDA(cudaSetDevice(b->device));
@@ -987,13 +924,29 @@ int pf_batch_records(pf_batch* b, int run, int first, int n, pf_diag* out) {
   for (int s = 0; s < n;) {
     const int pos = (first + s) % b->ring, take = std::min(n - s, b->ring - pos);
     PF_CUDA(cudaMemcpyAsync(h.data() + (size_t)s * DR_COUNT, ring + (size_t)pos * DR_COUNT,
-                            (size_t)take * DR_COUNT * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+                            (size_t)take * DR_COUNT * sizeof(double), cudaMemcpyDeviceToHost, b->copy));
     s += take;
   }
-  PF_CUDA(cudaStreamSynchronize(b->stream));
+  PF_CUDA(cudaStreamSynchronize(b->copy));
   for (int s = 0; s < n; ++s) fill_diag(h.data() + (size_t)s * DR_COUNT, &out[s]);
   return PF_OK;
 }
+// The k = 0 coefficient of run `run`'s concentration state (the mean of c,
+// f_trans normalisation): Re and Im as doubles.  The semi-implicit update
+// leaves this coefficient untouched, so the mass N^3 Re c_hat(0) is constant.
+int pf_batch_c_mean(pf_batch* b, int run, double* re_im) {
+  if (!b || run < 0 || run >= b->nruns || !re_im) return fail(PF_EINVAL, "bad arguments");
+  PF_CUDA(cudaSetDevice(b->device));
+  PF_CUDA(cudaStreamSynchronize(b->stream));
+  float2 v;
+  const size_t fieldc = (size_t)b->Kx * b->Ny * b->Nz;
+  PF_CUDA(cudaMemcpy(&v, b->hrp[run].Sk + (size_t)b->V * fieldc, sizeof v, cudaMemcpyDeviceToHost));
+  re_im[0] = v.x;
+  re_im[1] = v.y;
+  return PF_OK;
+}
+// Length of a batch's per-run record ring (steps whose records stay readable).
+int pf_batch_ring(pf_batch* b) { return b ? b->ring : 0; }
 // Number of compiled x-pass and yz-pass variants of a grid (the index range
 // of PFGPU_X_VARIANT / PFGPU_YZ_VARIANT).
 void pf_variant_counts(int nx, int ny, int nz, int* nxv, int* nyzv) {

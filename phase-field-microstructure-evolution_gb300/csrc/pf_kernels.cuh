@@ -56,6 +56,7 @@ struct RunParams {
   double* part_yz; // [nblk_yz]
   double* diag;    // [ring][DR_COUNT]
   int* counter;    // step counter (device)
+  unsigned* ticket;  // CTAs of the step's yz pass that have finished (reset by the last one)
   float* fin;      // [nF][Nz][Ny][Nx] real fields for import/export
   float L, kappa_phi, kappa_c, dt, D_L, D_gb, sigma1, sigma2, am, ap, c0m, c0p;
   int mobility;
@@ -96,6 +97,58 @@ __device__ __forceinline__ float warp_sumf(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// ---------------------------------------------------------------------------
+// Compensated sums for the mass of c (src/var_diff.f90:1076-1102).  A thread
+// keeps its running sum as an unevaluated FP32 pair hi + lo updated with
+// Knuth's error-free TwoSum (s + e == a + b exactly), warps combine the pairs
+// the same way, and from there on the sum is FP64 with Neumaier's
+// compensation (KSum) across warps, blocks and the final record.  FP64
+// arithmetic is scarce on this part, so only the per-warp and later stages
+// use it.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+struct FF {
+  float hi, lo;
+  __device__ __forceinline__ void add(float v) {
+    float s, e;
+    two_sum(hi, v, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, e);
+  }
+};
+// sum of the pairs of a warp (every lane gets the same value)
+__device__ __forceinline__ double warp_sum_ff(FF x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float bh = __shfl_xor_sync(0xffffffffu, x.hi, o), bl = __shfl_xor_sync(0xffffffffu, x.lo, o);
+    float s, e;
+    two_sum(x.hi, bh, s, e);
+    x.hi = s;
+    x.lo = __fadd_rn(__fadd_rn(x.lo, bl), e);
+  }
+  return (double)x.hi + (double)x.lo;
+}
+// compensated FP64 sum (Kahan-Babuska-Neumaier, the error of each addition
+// taken exactly by TwoSum): value() = s + c
+struct KSum {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double v) {
+    const double t = __dadd_rn(s, v);
+    const double bb = __dsub_rn(t, s);
+    c = __dadd_rn(c, __dadd_rn(__dsub_rn(s, __dsub_rn(t, bb)), __dsub_rn(v, bb)));
+    s = t;
+  }
+  __device__ __forceinline__ void add(const KSum& o) {
+    add(o.s);
+    c = __dadd_rn(c, o.c);
+  }
+  __device__ __forceinline__ double value() const { return __dadd_rn(s, c); }
+};
+
 __device__ __forceinline__ float warp_min(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -288,9 +341,15 @@ __device__ __forceinline__ void x_fwd_runs(float2* __restrict__ dst, size_t plan
 // fields.
 // ---------------------------------------------------------------------------
 struct BulkAcc {
-  float feta, fch, mass;  // per-thread partial sums over a few cells (FP64 from the warp level up)
+  float feta, fch;  // per-thread partial sums over a few cells (FP64 from the warp level up)
+  FF mass;          // compensated (exact) per-thread sum of c
   float cmin, cmax, phimin, phipmax;
   int nonfinite;
+  __device__ __forceinline__ void init() {
+    feta = 0.f; fch = 0.f; mass.hi = 0.f; mass.lo = 0.f;
+    cmin = 1.0f; cmax = 0.0f; phimin = 1.0f; phipmax = 0.0f;  // reference start values (:1076-1079)
+    nonfinite = 0;
+  }
 };
 
 // Bulk terms of the two cells x = 2m, 2m+1 held in one float2 slot of every
@@ -367,7 +426,7 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
     acc.fch += h * fm + (1.f - h) * fp;
     const float dc = 2.f * h * rp.am * dcm + 2.f * (1.f - h) * rp.ap * dcp;
     acc.feta += -0.5f * S2 + 0.25f * S4 + sg1 * pairs + sg2 * pp2 * pre;
-    acc.mass += c;
+    acc.mass.add(c);
     acc.cmin = fminf(acc.cmin, c);
     acc.cmax = fmaxf(acc.cmax, c);
     acc.phimin = fminf(acc.phimin, S2);
@@ -408,6 +467,48 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
     base[(V - 1) * FS] = make_float2(d0, d1);
   }
   acc.nonfinite += !isfinite(dsum);  // any NaN/Inf term makes the sum non-finite
+}
+
+// Block reduction of the x pass's diagnostics into the block's partials
+// part_x[q * nblk_x + blk] (all threads of the block call it).
+template <int T>
+__device__ __forceinline__ void store_block_diag(const BulkAcc& acc, const RunParams& rp, const Shape& sh, int blk) {
+  static_assert(T % 32 == 0 && T <= 1024, "whole warps");
+  __shared__ double red_d[3][T / 32];  // one slot per warp
+  __shared__ float red_f[4][T / 32];
+  __shared__ int red_i[T / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const double s0 = warp_sum((double)acc.feta), s1 = warp_sum((double)acc.fch), s2 = warp_sum_ff(acc.mass);
+  const float m0 = warp_min(acc.cmin), m1 = warp_max(acc.cmax), m2 = warp_min(acc.phimin), m3 = warp_max(acc.phipmax);
+  const int nb = __reduce_add_sync(0xffffffffu, acc.nonfinite);
+  if (lane == 0) {
+    red_d[0][wid] = s0; red_d[1][wid] = s1; red_d[2][wid] = s2;
+    red_f[0][wid] = m0; red_f[1][wid] = m1; red_f[2][wid] = m2; red_f[3][wid] = m3;
+    red_i[wid] = nb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a0 = 0, a1 = 0;
+    KSum a2;
+    float b0 = red_f[0][0], b1 = red_f[1][0], b2 = red_f[2][0], b3 = red_f[3][0];
+    int nn = 0;
+    for (int w = 0; w < T / 32; ++w) {
+      a0 += red_d[0][w]; a1 += red_d[1][w]; a2.add(red_d[2][w]);
+      b0 = fminf(b0, red_f[0][w]); b1 = fmaxf(b1, red_f[1][w]);
+      b2 = fminf(b2, red_f[2][w]); b3 = fmaxf(b3, red_f[3][w]);
+      nn += red_i[w];
+    }
+    const int nbk = sh.nblk_x;
+    double* p = rp.part_x + blk;
+    p[XD_FETA * nbk] = a0;
+    p[XD_FCH * nbk] = a1;
+    p[XD_MASS * nbk] = a2.value();
+    p[XD_CMIN * nbk] = b0;
+    p[XD_CMAX * nbk] = b1;
+    p[XD_PHIMIN * nbk] = b2;
+    p[XD_PHIPMAX * nbk] = b3;
+    p[XD_NONFINITE * nbk] = nn;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -466,9 +567,7 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
   }
 
   BulkAcc acc;
-  acc.feta = 0.f; acc.fch = 0.f; acc.mass = 0.f;
-  acc.cmin = 1.0f; acc.cmax = 0.0f; acc.phimin = 1.0f; acc.phipmax = 0.0f;  // reference start values
-  acc.nonfinite = 0;
+  acc.init();
 
   if (MODE == MODE_BULK) {
     // 2. bulk terms, two cells per slot
@@ -509,42 +608,7 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
   if (MODE != MODE_BULK) return;
 
   // 6. diagnostics: block reduction into per-block partials
-  static_assert(T % 32 == 0 && T <= 1024, "whole warps");
-  __shared__ double red_d[3][T / 32];  // one slot per warp
-  __shared__ float red_f[4][T / 32];
-  __shared__ int red_i[T / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double s0 = warp_sum((double)acc.feta), s1 = warp_sum((double)acc.fch), s2 = warp_sum((double)acc.mass);
-  float m0 = warp_min(acc.cmin), m1 = warp_max(acc.cmax), m2 = warp_min(acc.phimin), m3 = warp_max(acc.phipmax);
-  int nb = __reduce_add_sync(0xffffffffu, acc.nonfinite);
-  if (lane == 0) {
-    red_d[0][wid] = s0; red_d[1][wid] = s1; red_d[2][wid] = s2;
-    red_f[0][wid] = m0; red_f[1][wid] = m1; red_f[2][wid] = m2; red_f[3][wid] = m3;
-    red_i[wid] = nb;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nw = blockDim.x >> 5;
-    double a0 = 0, a1 = 0, a2 = 0;
-    float b0 = red_f[0][0], b1 = red_f[1][0], b2 = red_f[2][0], b3 = red_f[3][0];
-    int nn = 0;
-    for (int w = 0; w < nw; ++w) {
-      a0 += red_d[0][w]; a1 += red_d[1][w]; a2 += red_d[2][w];
-      b0 = fminf(b0, red_f[0][w]); b1 = fmaxf(b1, red_f[1][w]);
-      b2 = fminf(b2, red_f[2][w]); b3 = fmaxf(b3, red_f[3][w]);
-      nn += red_i[w];
-    }
-    const int nbk = sh.nblk_x;
-    double* p = rp.part_x + blockIdx.x;
-    p[XD_FETA * nbk] = a0;
-    p[XD_FCH * nbk] = a1;
-    p[XD_MASS * nbk] = a2;
-    p[XD_CMIN * nbk] = b0;
-    p[XD_CMAX * nbk] = b1;
-    p[XD_PHIMIN * nbk] = b2;
-    p[XD_PHIPMAX * nbk] = b3;
-    p[XD_NONFINITE * nbk] = nn;
-  }
+  store_block_diag<T>(acc, rp, sh, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -672,6 +736,105 @@ __device__ __forceinline__ void kpoint(const KPlane& P, const KRow& R, const flo
     const float sg = __fdividef(P.b * (R.g + z.z), fmaf(P.a, R.q4 + z.y, 1.0f));
     u = cadd(uu, cmul_pi(make_float2(d.x * sg, d.y * sg)));
   }
+}
+
+// ---------------------------------------------------------------------------
+// The step's record (src/var_diff.f90:1058-1118) is formed at the end of the
+// yz pass, with no separate launch: every CTA of a run's YZ_MAIN launches
+// stores its f_int partial and draws a ticket; the CTA that draws the last
+// one reduces the x-pass partials and all f_int partials of the run in a
+// fixed order (the result does not depend on which CTA comes last), writes the
+// record into the ring, advances the step counter and resets the ticket.
+// The c planes may run as a second, concurrent launch: both draw from the
+// run's one ticket counter, sized for all nblk_yz CTAs.
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ __noinline__ void step_record(const RunParams& rp, const Shape& sh) {
+  static_assert(T % 32 == 0 && T <= 1024, "whole warps");
+  __shared__ double sd[6][T / 32];  // f_eta, f_ch, mass (s, c), f_int, non-finite count
+  __shared__ float sf[4][T / 32];
+  __threadfence();
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int nb = sh.nblk_x;
+  const double* __restrict__ px = rp.part_x;
+  double a_eta = 0, a_ch = 0, a_int = 0, a_bad = 0;
+  KSum a_mass;
+  float cmin = 1.f, cmax = 0.f, pmin = 1.f, ppmax = 0.f;  // reference start values (:1076-1079)
+  for (int i = t; i < nb; i += T) {
+    a_eta += __ldcg(px + XD_FETA * nb + i);
+    a_ch += __ldcg(px + XD_FCH * nb + i);
+    a_mass.add(__ldcg(px + XD_MASS * nb + i));
+    cmin = fminf(cmin, (float)__ldcg(px + XD_CMIN * nb + i));
+    cmax = fmaxf(cmax, (float)__ldcg(px + XD_CMAX * nb + i));
+    pmin = fminf(pmin, (float)__ldcg(px + XD_PHIMIN * nb + i));
+    ppmax = fmaxf(ppmax, (float)__ldcg(px + XD_PHIPMAX * nb + i));
+    a_bad += __ldcg(px + XD_NONFINITE * nb + i);
+  }
+  for (int i = t; i < sh.nblk_yz; i += T) a_int += __ldcg(rp.part_yz + i);
+  a_eta = warp_sum(a_eta); a_ch = warp_sum(a_ch); a_int = warp_sum(a_int); a_bad = warp_sum(a_bad);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    KSum other;
+    other.s = __shfl_xor_sync(0xffffffffu, a_mass.s, o);
+    other.c = __shfl_xor_sync(0xffffffffu, a_mass.c, o);
+    a_mass.add(other);
+  }
+  cmin = warp_min(cmin); cmax = warp_max(cmax); pmin = warp_min(pmin); ppmax = warp_max(ppmax);
+  if (lane == 0) {
+    sd[0][w] = a_eta; sd[1][w] = a_ch; sd[2][w] = a_mass.s; sd[3][w] = a_mass.c; sd[4][w] = a_int; sd[5][w] = a_bad;
+    sf[0][w] = cmin; sf[1][w] = cmax; sf[2][w] = pmin; sf[3][w] = ppmax;
+  }
+  __syncthreads();
+  if (t == 0) {
+    double e = 0, c = 0, fi = 0, bad = 0;
+    KSum m;
+    float m0 = 1.f, m1 = 0.f, m2 = 1.f, m3 = 0.f;
+    for (int k = 0; k < T / 32; ++k) {
+      e += sd[0][k]; c += sd[1][k]; fi += sd[4][k]; bad += sd[5][k];
+      KSum o;
+      o.s = sd[2][k];
+      o.c = sd[3][k];
+      m.add(o);
+      m0 = fminf(m0, sf[0][k]); m1 = fmaxf(m1, sf[1][k]); m2 = fminf(m2, sf[2][k]); m3 = fmaxf(m3, sf[3][k]);
+    }
+    const int step = *rp.counter;
+    double* d = rp.diag + (size_t)(step % rp.ring) * DR_COUNT;
+    d[DR_STEP] = step + 1;
+    d[DR_FINT] = fi;
+    d[DR_FETA] = e;
+    d[DR_FCH] = c;
+    d[DR_CMIN] = m0;
+    d[DR_CMAX] = m1;
+    d[DR_PHIMIN] = m2;
+    d[DR_PHIPMAX] = m3;
+    d[DR_MASS] = m.value();
+    d[DR_NONFINITE] = bad;
+    *rp.counter = step + 1;
+    *rp.ticket = 0u;  // the next step's yz pass starts after this launch ends
+  }
+}
+
+// Store this CTA's f_int partial (coef times the block sum of the per-thread
+// FP32 sums) in slot `slot`, then draw the ticket; the last CTA forms the record.
+template <int T>
+__device__ __forceinline__ void yz_finish(const RunParams& rp, const Shape& sh, float fint, double coef, size_t slot) {
+  __shared__ double red[T / 32];
+  __shared__ int last;
+  const double v = (double)warp_sumf(fint);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+#pragma unroll
+    for (int q = 0; q < T / 32; ++q) s += red[q];
+    rp.part_yz[slot] = s * coef;
+    __threadfence();
+    const unsigned tk = atomicAdd(rp.ticket, 1u);
+    last = (tk + 1u == (unsigned)sh.nblk_yz);
+  }
+  __syncthreads();
+  if (last) step_record<T>(rp, sh);
 }
 
 template <int C>
@@ -829,7 +992,6 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   constexpr int N1y = LY::N1, N2y = LY::N2, N1z = LZ::N1, N2z = LZ::N2;
   static_assert(T % N1y == 0 && T % N2z == 0, "thread count");
   extern __shared__ float2 smem[];
-  __shared__ double red[T / 32];
   __shared__ float4 qzt[NZ];  // kz factors of the k-space update
   stage_kz<NZ, T>(qzt, sh);   // read after the barriers of the forward passes
   float2* UA = smem;
@@ -970,18 +1132,9 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
 
   if (MODE == YZ_MAIN) {
     // f_int partial (:609-678 by Parseval): 0.5 kappa N^3 w |kf|^2 |u_hat|^2
-    const double v = (double)warp_sumf(fint);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0;
-#pragma unroll
-      for (int w = 0; w < T / 32; ++w) s += red[w];
-      const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
-      const double n3 = (double)sh.Nx * NY * NZ;
-      rp.part_yz[(size_t)sh.plane0 * C + blockIdx.x] = s * wkx * 0.5 * kap * n3;
-    }
+    const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
+    const double n3 = (double)sh.Nx * NY * NZ;
+    yz_finish<T>(rp, sh, fint, wkx * 0.5 * kap * n3, (size_t)sh.plane0 * C + blockIdx.x);
   }
 }
 
@@ -1041,7 +1194,6 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   constexpr int PY = YZ1<NY, NZ, RAWP>::PY;
   static_assert(T % N1y == 0 && T % N2y == 0, "thread count");
   extern __shared__ float2 U[];
-  __shared__ double red[T / 32];
   __shared__ float4 qzt[NZ];  // kz factors of the k-space update
   stage_kz<NZ, T>(qzt, sh);   // read after the barriers of the forward passes
   const RunParams& rp = runs[blockIdx.y];
@@ -1164,18 +1316,9 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   }
 
   if (MODE == YZ_MAIN) {
-    const double v = (double)warp_sumf(fint);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0;
-#pragma unroll
-      for (int q = 0; q < T / 32; ++q) s += red[q];
-      const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
-      const double n3 = (double)sh.Nx * NY * NZ;
-      rp.part_yz[p] = s * wkx * 0.5 * kap * n3;
-    }
+    const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
+    const double n3 = (double)sh.Nx * NY * NZ;
+    yz_finish<T>(rp, sh, fint, wkx * 0.5 * kap * n3, (size_t)p);
   }
 }
 
@@ -1240,7 +1383,7 @@ __device__ __forceinline__ CellOut cell_terms(float pp, float c, float pre, floa
   CellOut o;
   o.dc = 2.f * h * rp.am * dcm + 2.f * (1.f - h) * rp.ap * dcp;
   acc.feta += -0.5f * S2 + 0.25f * S4 + rp.sigma1 * pairs + rp.sigma2 * pp2 * pre;
-  acc.mass += c;
+  acc.mass.add(c);
   acc.cmin = fminf(acc.cmin, c);
   acc.cmax = fmaxf(acc.cmax, c);
   acc.phimin = fminf(acc.phimin, S2);
@@ -1372,9 +1515,7 @@ __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restric
 
   // 4. per-cell scalars and dF of the local fields, in place
   BulkAcc acc;
-  acc.feta = 0.f; acc.fch = 0.f; acc.mass = 0.f;
-  acc.cmin = 1.0f; acc.cmax = 0.0f; acc.phimin = 1.0f; acc.phipmax = 0.0f;  // reference start values
-  acc.nonfinite = 0;
+  acc.init();
   const float sg1 = rp.sigma1, sg2 = rp.sigma2;
   for (int it = threadIdx.x; it < S; it += T) {
     const int m = it % M, yy = it / M;
@@ -1424,40 +1565,7 @@ __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restric
   if (!rank) return;
 
   // 6. diagnostics (rank 1): block reduction into the pair's partials
-  __shared__ double red_d[3][T / 32];
-  __shared__ float red_f[4][T / 32];
-  __shared__ int red_i[T / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double s0 = warp_sum((double)acc.feta), s1 = warp_sum((double)acc.fch), s2 = warp_sum((double)acc.mass);
-  float m0 = warp_min(acc.cmin), m1 = warp_max(acc.cmax), m2 = warp_min(acc.phimin), m3 = warp_max(acc.phipmax);
-  int nb = __reduce_add_sync(0xffffffffu, acc.nonfinite);
-  if (lane == 0) {
-    red_d[0][wid] = s0; red_d[1][wid] = s1; red_d[2][wid] = s2;
-    red_f[0][wid] = m0; red_f[1][wid] = m1; red_f[2][wid] = m2; red_f[3][wid] = m3;
-    red_i[wid] = nb;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a0 = 0, a1 = 0, a2 = 0;
-    float b0 = red_f[0][0], b1 = red_f[1][0], b2 = red_f[2][0], b3 = red_f[3][0];
-    int nn = 0;
-    for (int w = 0; w < T / 32; ++w) {
-      a0 += red_d[0][w]; a1 += red_d[1][w]; a2 += red_d[2][w];
-      b0 = fminf(b0, red_f[0][w]); b1 = fmaxf(b1, red_f[1][w]);
-      b2 = fminf(b2, red_f[2][w]); b3 = fmaxf(b3, red_f[3][w]);
-      nn += red_i[w];
-    }
-    const int nbk = sh.nblk_x;
-    double* p = rp.part_x + bp;
-    p[XD_FETA * nbk] = a0;
-    p[XD_FCH * nbk] = a1;
-    p[XD_MASS * nbk] = a2;
-    p[XD_CMIN * nbk] = b0;
-    p[XD_CMAX * nbk] = b1;
-    p[XD_PHIMIN * nbk] = b2;
-    p[XD_PHIPMAX * nbk] = b3;
-    p[XD_NONFINITE * nbk] = nn;
-  }
+  store_block_diag<T>(acc, rp, sh, bp);
 }
 
 }  // namespace pf

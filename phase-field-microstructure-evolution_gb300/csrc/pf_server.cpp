@@ -42,6 +42,7 @@ void* pf_batch_stream(pf_batch* b);
 size_t pf_batch_bytes(const pf_config* c, int nruns);
 int pf_batch_steps_done(pf_batch* b, int run);
 int pf_batch_records(pf_batch* b, int run, int first, int n, pf_diag* out);
+int pf_batch_ring(pf_batch* b);
 }
 
 namespace {
@@ -73,6 +74,11 @@ struct Chunk {
 };
 
 constexpr int kInFlight = 2;  // chunks queued per batch, so the GPU has work while the worker is busy
+constexpr int kRing = 1024;   // per-run record ring of a batch (pf_batch_ring)
+// Longest chunk: the records of all chunks in flight must fit the ring at
+// once, since the newest chunk writes its slots while the oldest one's are
+// copied out.
+constexpr int kMaxChunk = kRing / kInFlight;
 
 struct Active {
   pf_batch* b = nullptr;
@@ -160,6 +166,11 @@ void admit(pf_server* s) {
     for (auto& r : group) cfgs.push_back(r->cfg);
     Active a;
     int rc = pf_batch_create(cfgs.data(), (int)cfgs.size(), &a.b);
+    std::string msg;
+    if (rc == PF_OK && pf_batch_ring(a.b) < kRing) {
+      rc = PF_EINVAL;
+      msg = "record ring shorter than the server's chunks need";
+    }
     for (size_t i = 0; rc == PF_OK && i < group.size(); ++i)
       rc = pf_batch_set_fields(a.b, (int)i, group[i]->phi.data(), group[i]->con.data());
     for (int k = 0; rc == PF_OK && k < kInFlight; ++k) {
@@ -168,7 +179,7 @@ void admit(pf_server* s) {
       else a.spare.push_back(ev);
     }
     if (rc != PF_OK) {
-      const std::string msg = pf_last_error();
+      if (msg.empty()) msg = pf_last_error();
       if (a.b) pf_batch_destroy(a.b);
       for (cudaEvent_t ev : a.spare) cudaEventDestroy(ev);
       for (auto& r : group) finish(s, *r, PF_REQ_FAILED, rc, msg);
@@ -316,7 +327,7 @@ int pf_server_create(const pf_server_config* cfg, pf_server** out) {
   if (cfg) s->cfg = *cfg;
   if (s->cfg.max_active <= 0) s->cfg.max_active = 64;
   if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 128;
-  s->cfg.chunk_steps = std::min(s->cfg.chunk_steps, 1024);  // the per-run record ring
+  s->cfg.chunk_steps = std::min(s->cfg.chunk_steps, kMaxChunk);
   cudaError_t e = cudaSetDevice(s->cfg.device);
   size_t free_b = 0, total_b = 0;
   if (e == cudaSuccess) e = cudaMemGetInfo(&free_b, &total_b);

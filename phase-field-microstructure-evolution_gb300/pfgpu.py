@@ -149,6 +149,8 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_batch_stream": (C.c_void_p, [C.c_void_p]),
         "pf_batch_variant": (C.c_char_p, [C.c_void_p]),
         "pf_run_batch": (C.c_void_p, [C.c_void_p]),
+        "pf_batch_c_mean": (C.c_int, [C.c_void_p, C.c_int, dp]),
+        "pf_batch_ring": (C.c_int, [C.c_void_p]),
         "pf_variant_counts": (None, [C.c_int, C.c_int, C.c_int, ip, ip]),
         "f_trans_": (None, [dp, dp, ip, ip, ip, ip, ip, ip, ip]),
         "inv_trans_": (None, [dp, dp, ip, ip, ip, ip]),
@@ -264,6 +266,13 @@ class Run:
 
     def batch_handle(self):
         return self.lib.pf_run_batch(self.h)
+
+    def c_mean(self) -> complex:
+        """The k = 0 coefficient of the resident concentration state (fused
+        path): the mean of c, so N^3 times its real part is the mass."""
+        v = (C.c_double * 2)()
+        _check(self.lib.pf_batch_c_mean(self.batch_handle(), 0, v))
+        return complex(v[0], v[1])
 
     def close(self):
         if getattr(self, "h", None):

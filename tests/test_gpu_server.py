@@ -81,3 +81,24 @@ def test_server_budget_and_states(pkg, oracle):
             srv.poll(a)  # forgotten after wait
     finally:
         srv.close()
+
+
+def test_server_long_chunks_keep_their_records(pkg, oracle):
+    """chunk_steps above 512 is cut to 512, so that the records of the two
+    chunks kept in flight both fit the per-run ring of 1024: the last record
+    and the fields of a 1500-step run equal those of the run alone."""
+    p = oracle.Params(16, 16, 16, 3, t_step=0.05)
+    phi, con = oracle.ic_noise(p, 9, 0.001, 0.5, 0.01)
+    srv = pkg.Server(chunk_steps=1000)
+    try:
+        rid = srv.submit(p, phi, con, 1500)
+        gp, gc, last, _ = srv.wait(rid, timeout=600.0)
+    finally:
+        srv.close()
+    run = pkg.Run(p)
+    run.set_fields(phi, con)
+    d = run.step(1500)
+    ap, ac = run.get_fields()
+    run.close()
+    assert np.array_equal(gp, ap) and np.array_equal(gc, ac)
+    assert last == d[-1], (last, d[-1])
