@@ -610,6 +610,13 @@ def _pct(xs, q):
 
 
 def run_serve(args):
+    """Config 4 at every rate of --rates: the served stream (submitted at its
+    Poisson arrival times to a pf_pool -- one continuous-batching pf_server
+    per visible GPU) against serial execution of the same requests.  The
+    request properties come from the same ran_2 draws at every rate; only the
+    arrival times scale with 1/rate.  Serial: each request's service time alone
+    (pf_create / pf_set_fields / pf_step / pf_get_fields, measured once),
+    replayed as a FIFO single server at each rate's arrival times."""
     import torch
 
     torch.cuda.set_device(0)
@@ -617,51 +624,61 @@ def run_serve(args):
     import __graft_entry__ as ge
 
     pkg = ge.load_package()
-    reqs = serve_requests(pkg, args.requests, args.rate)
-    starts = [pkg.ic_noise(p, seed, 0.001, c0, 0.01) for (_, p, _, seed, c0) in reqs]
+    rates = [float(r) for r in str(args.rates).split(",")] if args.rates else [args.rate]
+    base = serve_requests(pkg, args.requests, 1.0)  # arrival times at rate 1; scaled per rate below
+    starts = [pkg.ic_noise(p, seed, 0.001, c0, 0.01) for (_, p, _, seed, c0) in base]
     # warm the autotuner cache for every class (as a long-running server would be)
-    for cls in sorted({(p.Nx, p.var) for (_, p, _, _, _) in reqs}):
-        p = next(r[1] for r in reqs if (r[1].Nx, r[1].var) == cls)
+    for cls in sorted({(p.Nx, p.var) for (_, p, _, _, _) in base}):
+        p = next(r[1] for r in base if (r[1].Nx, r[1].var) == cls)
         w = pkg.Run(p)
         w.close()
     torch.cuda.synchronize()
-    # served: submit at the arrival times, overlap on the device
-    srv = pkg.Server(max_active=args.max_active)
-    t0 = time.perf_counter()
-    ids = []
-    for (ta, p, steps, _, _), (phi, con) in zip(reqs, starts):
-        while time.perf_counter() - t0 < ta:
-            time.sleep(0.0005)
-        ids.append(srv.submit(p, phi, con, steps))
-    lat = []
-    for i in ids:
-        _, _, _, tm = srv.wait(i)
-        lat.append(tm["total_s"])
-    t_served = time.perf_counter() - t0
-    srv.close()
-    # serial: the same stream, one run at a time in arrival order
-    clock, lat_s = 0.0, []
-    for (ta, p, steps, _, _), (phi, con) in zip(reqs, starts):
+    # serial service times, measured once
+    service = []
+    for (_, p, steps, _, _), (phi, con) in zip(base, starts):
         run = pkg.Run(p)
         tb = time.perf_counter()
         run.set_fields(phi, con)
         run.step(steps, raise_nonfinite=False)
         run.get_fields()
-        dt = time.perf_counter() - tb
+        service.append(time.perf_counter() - tb)
         run.close()
-        clock = max(clock, ta) + dt
-        lat_s.append(clock - ta)
-    n = len(reqs)
-    work = sum(p.Nx * p.Ny * p.Nz * p.var * steps for (_, p, steps, _, _) in reqs)
-    line = {"metric": "served runs/s", "value": n / t_served, "unit": "runs/s", "n_gpus": 1, "steps": None,
-            "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic request stream (ran_2 seed 4)",
-            "config": {"workload": f"served stream: {n} requests, Poisson rate {args.rate}/s, grids 32-256, "
+    n = len(base)
+    work = sum(p.Nx * p.Ny * p.Nz * p.var * steps for (_, p, steps, _, _) in base)
+    per_rate = []
+    for rate in rates:
+        arrivals = [ta / rate for (ta, _, _, _, _) in base]
+        pool = pkg.Pool(max_active=args.max_active)
+        t0 = time.perf_counter()
+        ids = []
+        for ta, (_, p, steps, _, _), (phi, con) in zip(arrivals, base, starts):
+            while time.perf_counter() - t0 < ta:
+                time.sleep(0.0005)
+            ids.append(pool.submit(p, phi, con, steps)[0])
+        lat = []
+        for i in ids:
+            _, _, _, tm = pool.wait(i)
+            lat.append(tm["total_s"])
+        t_served = time.perf_counter() - t0
+        ndev = pool.devices
+        pool.close()
+        clock, lat_s = 0.0, []
+        for ta, dt in zip(arrivals, service):
+            clock = max(clock, ta) + dt
+            lat_s.append(clock - ta)
+        per_rate.append({"rate_per_s": rate, "devices": ndev,
+                         "served": {"runs_per_s": n / t_served, "p50_s": _pct(lat, 0.5), "p99_s": _pct(lat, 0.99),
+                                    "cell_steps_per_s_x_P": work / t_served},
+                         "serial": {"runs_per_s": n / clock, "p50_s": _pct(lat_s, 0.5), "p99_s": _pct(lat_s, 0.99)}})
+    top = per_rate[-1]
+    line = {"metric": "served runs/s", "value": top["served"]["runs_per_s"], "unit": "runs/s", "n_gpus": top["devices"],
+            "steps": None, "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic request stream (ran_2 seed 4)",
+            "config": {"workload": f"served stream: {n} requests per rate, Poisson rates {rates}/s, grids 32-256, "
                                    f"P 4-16, 100-5000 steps (config 4)", "max_active": args.max_active},
-            "latency_s": {"p50": _pct(lat, 0.5), "p99": _pct(lat, 0.99)},
-            "cell_steps_per_s_x_P": work / t_served,
-            "serial": {"runs_per_s": n / clock, "latency_s": {"p50": _pct(lat_s, 0.5), "p99": _pct(lat_s, 0.99)},
-                       "what": "the same requests one at a time in arrival order (pf_create/pf_step)"}}
+            "rates": per_rate,
+            "serial_what": "each request alone (pf_create/pf_set_fields/pf_step/pf_get_fields), service times "
+                           "measured once, FIFO single server at each rate's arrival times"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -685,6 +702,8 @@ def main():
     ap.add_argument("--runs", type=int, default=256, help="ensemble: runs in the batch")
     ap.add_argument("--requests", type=int, default=24, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=8.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--rates", type=str, default=None,
+                    help="serve: comma-separated arrival rates to sweep (requests/s), e.g. 2,4,8,16")
     ap.add_argument("--max-active", type=int, default=16, help="serve: resident runs at most")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -165,6 +165,39 @@ int pf_server_destroy(pf_server* s);
 /* Message of the last failed pf_server_* call of the calling thread. */
 const char* pf_server_last_error(void);
 
+/* ---- independent runs over the node's GPUs (no collective) ----------------
+ * The reference fans a study out as one SLURM job per run
+ * (tests/scaling_tests.py:88-124, tests/run_phase_sim.py:130-172).  Here runs
+ * never exchange data, so the GPUs of a node share the work only through
+ * placement: one pf_server per device, each request sent to the device with
+ * the least outstanding work (cell-steps x P of its unfinished requests). */
+/* Visible CUDA devices (0 without a GPU). */
+int pf_device_count(void);
+/* Work of a run: nx ny nz var nsteps (cell-steps x P). */
+double pf_run_work(const pf_config* cfg, int nsteps);
+/* Online placement: index of the smallest outstanding[d] (ties: lowest d). */
+int pf_pick_device(const double* outstanding, int ndev);
+/* Offline placement of nunits work units (LPT): largest unit first onto the
+ * device with the least work so far.  device_of_unit[u] in [0, ndev); load
+ * (may be NULL) receives the work per device. */
+int pf_place_units(const double* work, int nunits, int ndev, int* device_of_unit, double* load);
+typedef struct pf_pool pf_pool;
+typedef struct pf_pool_config {
+  int ndevices;            /* devices to use (0: every visible device) */
+  const int* devices;      /* their ordinals (NULL: 0 .. ndevices-1) */
+  pf_server_config server; /* settings of every device's server (its device field is ignored) */
+} pf_pool_config;
+int pf_pool_create(const pf_pool_config* cfg, pf_pool** out);
+int pf_pool_devices(pf_pool* p);
+/* As pf_server_submit; *device (may be NULL) receives the chosen ordinal. */
+int pf_pool_submit(pf_pool* p, const pf_config* cfg, const double* phi_aos, const double* con, int nsteps,
+                   long long* id, int* device);
+/* As pf_server_wait. */
+int pf_pool_wait(pf_pool* p, long long id, double timeout_s, double* phi_aos, double* con, pf_diag* last,
+                 pf_request_times* times);
+int pf_pool_destroy(pf_pool* p);
+const char* pf_pool_last_error(void);
+
 /* ---- Fortran compatibility shims (single rank, FP64, whole grid) ---------
  * Same argument lists as the reference subroutines, all by reference, with
  * gfortran/ifort-on-Linux name mangling.  ist = (1,1,1), ien = (Nx,Ny,Nz);

@@ -14,7 +14,7 @@
 // takes that order back to natural order.  The spectral update in between is
 // pointwise, so no reordering pass is ever needed.
 //
-// Each DFT of size <= 16 lives in registers; in shared memory every run of N1
+// Each DFT of size <= 20 lives in registers; in shared memory every run of N1
 // consecutive elements is followed by one pad slot and the line pitch is odd,
 // which makes pass A, pass B and line-to-line transposes free of bank
 // conflicts for 8-byte complex elements.
@@ -23,22 +23,26 @@
 
 namespace pf {
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+// The in-register DFTs and complex helpers compile for the host as well, so
+// that tests can check them against a reference DFT on the CPU.
+#define PF_HD __host__ __device__ __forceinline__
+
+PF_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+PF_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+PF_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+PF_HD float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 // a * b
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+PF_HD float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 // a * conj(b)
-__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+PF_HD float2 cmulc(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
 }
 // -i * a
-__device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
+PF_HD float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
 // +i * a
-__device__ __forceinline__ float2 cmul_pi(float2 a) { return make_float2(-a.y, a.x); }
+PF_HD float2 cmul_pi(float2 a) { return make_float2(-a.y, a.x); }
 
 // ---------------------------------------------------------------------------
 // Exact twiddle constants for the in-register DFTs (W_R^j = e^{-2 pi i j / R})
@@ -47,32 +51,49 @@ __device__ __forceinline__ float2 cmul_pi(float2 a) { return make_float2(-a.y, a
 #define PF_S16_1 0.38268343236508977173f  // sin(pi/8)
 #define PF_SQRT1_2 0.70710678118654752440f
 #define PF_SQRT3_2 0.86602540378443864676f
+// cos(2 pi j / 20), j = 1..4 (the radix-5 stages)
+#define PF_C20_1 0.95105651629515357212f  // cos(pi/10)
+#define PF_C20_2 0.80901699437494742410f  // cos(pi/5)
+#define PF_C20_3 0.58778525229247312917f  // cos(3 pi/10)
+#define PF_C20_4 0.30901699437494742410f  // cos(2 pi/5)
 
-// W_R^j for R in {2,3,4,6,8,12,16} (forward sign), j in [0, R)
+// W_R^j for R in {2,3,4,5,6,8,10,12,16,20} (forward sign), j in [0, R)
 template <int R>
-__device__ __forceinline__ float2 wconst(int j);
+PF_HD float2 wconst(int j);
 
 template <>
-__device__ __forceinline__ float2 wconst<16>(int j) {
+PF_HD float2 wconst<16>(int j) {
   // angles j * 22.5 degrees, clockwise
   const float c[16] = {1.f, PF_C16_1, PF_SQRT1_2, PF_S16_1, 0.f, -PF_S16_1, -PF_SQRT1_2, -PF_C16_1,
                        -1.f, -PF_C16_1, -PF_SQRT1_2, -PF_S16_1, 0.f, PF_S16_1, PF_SQRT1_2, PF_C16_1};
   return make_float2(c[j & 15], -c[(j + 12) & 15]);
 }
 template <>
-__device__ __forceinline__ float2 wconst<8>(int j) { return wconst<16>(2 * j); }
+PF_HD float2 wconst<8>(int j) { return wconst<16>(2 * j); }
 template <>
-__device__ __forceinline__ float2 wconst<4>(int j) { return wconst<16>(4 * j); }
+PF_HD float2 wconst<4>(int j) { return wconst<16>(4 * j); }
 template <>
-__device__ __forceinline__ float2 wconst<12>(int j) {
+PF_HD float2 wconst<12>(int j) {
   // angles j * 30 degrees, clockwise
   const float c[12] = {1.f, PF_SQRT3_2, 0.5f, 0.f, -0.5f, -PF_SQRT3_2, -1.f, -PF_SQRT3_2, -0.5f, 0.f, 0.5f, PF_SQRT3_2};
   return make_float2(c[j % 12], -c[(j + 9) % 12]);
 }
 template <>
-__device__ __forceinline__ float2 wconst<6>(int j) { return wconst<12>(2 * j); }
+PF_HD float2 wconst<6>(int j) { return wconst<12>(2 * j); }
 template <>
-__device__ __forceinline__ float2 wconst<3>(int j) { return wconst<12>(4 * j); }
+PF_HD float2 wconst<20>(int j) {
+  // angles j * 18 degrees, clockwise
+  const float c[20] = {1.f,       PF_C20_1,  PF_C20_2,  PF_C20_3,  PF_C20_4,  0.f,       -PF_C20_4,
+                       -PF_C20_3, -PF_C20_2, -PF_C20_1, -1.f,      -PF_C20_1, -PF_C20_2, -PF_C20_3,
+                       -PF_C20_4, 0.f,       PF_C20_4,  PF_C20_3,  PF_C20_2,  PF_C20_1};
+  return make_float2(c[j % 20], -c[(j + 15) % 20]);
+}
+template <>
+PF_HD float2 wconst<10>(int j) { return wconst<20>(2 * j); }
+template <>
+PF_HD float2 wconst<5>(int j) { return wconst<20>(4 * j); }
+template <>
+PF_HD float2 wconst<3>(int j) { return wconst<12>(4 * j); }
 
 // ---------------------------------------------------------------------------
 // In-register forward DFTs, natural order in and out
@@ -82,12 +103,12 @@ struct Dft;
 
 template <>
 struct Dft<1> {
-  __device__ __forceinline__ static void fwd(float2*) {}
+  PF_HD static void fwd(float2*) {}
 };
 
 template <>
 struct Dft<2> {
-  __device__ __forceinline__ static void fwd(float2* v) {
+  PF_HD static void fwd(float2* v) {
     float2 a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
@@ -96,7 +117,7 @@ struct Dft<2> {
 
 template <>
 struct Dft<3> {
-  __device__ __forceinline__ static void fwd(float2* v) {
+  PF_HD static void fwd(float2* v) {
     float2 a = v[0];
     float2 t1 = cadd(v[1], v[2]);
     float2 t2 = csub(v[1], v[2]);
@@ -110,7 +131,7 @@ struct Dft<3> {
 
 template <>
 struct Dft<4> {
-  __device__ __forceinline__ static void fwd(float2* v) {
+  PF_HD static void fwd(float2* v) {
     float2 t0 = cadd(v[0], v[2]);
     float2 t1 = csub(v[0], v[2]);
     float2 t2 = cadd(v[1], v[3]);
@@ -122,11 +143,35 @@ struct Dft<4> {
   }
 };
 
+// Radix 5 from the pairs x1 +- x4, x2 +- x3:
+//   X0 = x0 + t1 + t2,  X1,4 = x0 + c1 t1 + c2 t2 -+ i (s1 d1 + s2 d2),
+//   X2,3 = x0 + c2 t1 + c1 t2 -+ i (s2 d1 - s1 d2),
+// with t1 = x1 + x4, t2 = x2 + x3, d1 = x1 - x4, d2 = x2 - x3,
+// c1 = cos(2 pi/5), c2 = cos(4 pi/5), s1 = sin(2 pi/5), s2 = sin(4 pi/5).
+template <>
+struct Dft<5> {
+  PF_HD static void fwd(float2* v) {
+    const float c1 = PF_C20_4, c2 = -PF_C20_2, s1 = PF_C20_1, s2 = PF_C20_3;
+    const float2 x0 = v[0];
+    const float2 t1 = cadd(v[1], v[4]), d1 = csub(v[1], v[4]);
+    const float2 t2 = cadd(v[2], v[3]), d2 = csub(v[2], v[3]);
+    const float2 a1 = make_float2(fmaf(c2, t2.x, fmaf(c1, t1.x, x0.x)), fmaf(c2, t2.y, fmaf(c1, t1.y, x0.y)));
+    const float2 a2 = make_float2(fmaf(c1, t2.x, fmaf(c2, t1.x, x0.x)), fmaf(c1, t2.y, fmaf(c2, t1.y, x0.y)));
+    const float2 b1 = make_float2(fmaf(s2, d2.x, s1 * d1.x), fmaf(s2, d2.y, s1 * d1.y));
+    const float2 b2 = make_float2(fmaf(-s1, d2.x, s2 * d1.x), fmaf(-s1, d2.y, s2 * d1.y));
+    v[0] = cadd(x0, cadd(t1, t2));
+    v[1] = cadd(a1, cmul_mi(b1));
+    v[4] = cadd(a1, cmul_pi(b1));
+    v[2] = cadd(a2, cmul_mi(b2));
+    v[3] = cadd(a2, cmul_pi(b2));
+  }
+};
+
 // Composite R = R1*R2 in registers: x[n1 + R1*n2] -> X[k2 + R2*k1]
 template <int R1, int R2>
 struct DftComposite {
   static constexpr int R = R1 * R2;
-  __device__ __forceinline__ static void fwd(float2* v) {
+  PF_HD static void fwd(float2* v) {
     float2 t[R];
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
@@ -154,24 +199,32 @@ struct DftComposite {
 
 template <>
 struct Dft<6> {
-  __device__ __forceinline__ static void fwd(float2* v) { DftComposite<2, 3>::fwd(v); }
+  PF_HD static void fwd(float2* v) { DftComposite<2, 3>::fwd(v); }
 };
 template <>
 struct Dft<8> {
-  __device__ __forceinline__ static void fwd(float2* v) { DftComposite<2, 4>::fwd(v); }
+  PF_HD static void fwd(float2* v) { DftComposite<2, 4>::fwd(v); }
 };
 template <>
 struct Dft<12> {
-  __device__ __forceinline__ static void fwd(float2* v) { DftComposite<4, 3>::fwd(v); }
+  PF_HD static void fwd(float2* v) { DftComposite<4, 3>::fwd(v); }
 };
 template <>
 struct Dft<16> {
-  __device__ __forceinline__ static void fwd(float2* v) { DftComposite<4, 4>::fwd(v); }
+  PF_HD static void fwd(float2* v) { DftComposite<4, 4>::fwd(v); }
+};
+template <>
+struct Dft<10> {
+  PF_HD static void fwd(float2* v) { DftComposite<2, 5>::fwd(v); }
+};
+template <>
+struct Dft<20> {
+  PF_HD static void fwd(float2* v) { DftComposite<4, 5>::fwd(v); }
 };
 
 // Inverse (unnormalised, e^{+2 pi i jk/R}) via conj(DFT(conj(x)))
 template <int R>
-__device__ __forceinline__ void dft_inv(float2* v) {
+PF_HD void dft_inv(float2* v) {
 #pragma unroll
   for (int i = 0; i < R; ++i) v[i].y = -v[i].y;
   Dft<R>::fwd(v);
@@ -191,11 +244,16 @@ template <> struct Plan<12>  { static constexpr int N1 = 4,  N2 = 3; };
 template <> struct Plan<16>  { static constexpr int N1 = 4,  N2 = 4; };
 template <> struct Plan<24>  { static constexpr int N1 = 8,  N2 = 3; };
 template <> struct Plan<32>  { static constexpr int N1 = 8,  N2 = 4; };
+template <> struct Plan<40>  { static constexpr int N1 = 8,  N2 = 5; };
 template <> struct Plan<48>  { static constexpr int N1 = 8,  N2 = 6; };
 template <> struct Plan<64>  { static constexpr int N1 = 8,  N2 = 8; };
+template <> struct Plan<80>  { static constexpr int N1 = 16, N2 = 5; };
 template <> struct Plan<96>  { static constexpr int N1 = 8,  N2 = 12; };
+template <> struct Plan<100> { static constexpr int N1 = 10, N2 = 10; };
 template <> struct Plan<128> { static constexpr int N1 = 16, N2 = 8; };
+template <> struct Plan<160> { static constexpr int N1 = 16, N2 = 10; };
 template <> struct Plan<192> { static constexpr int N1 = 16, N2 = 12; };
+template <> struct Plan<200> { static constexpr int N1 = 20, N2 = 10; };
 template <> struct Plan<256> { static constexpr int N1 = 16, N2 = 16; };
 
 template <int L>
@@ -206,10 +264,10 @@ struct Line {
   // padded storage: one pad slot after every run of N1, odd line pitch
   static constexpr int RAW = N2 * (N1 + 1);
   static constexpr int PITCH = (RAW % 2 == 1) ? RAW : RAW + 1;
-  __device__ __forceinline__ static int phys(int j) { return j + j / N1; }
+  PF_HD static int phys(int j) { return j + j / N1; }
   // frequency held at (natural) position p after a forward transform
-  __device__ __forceinline__ static int freq_of_pos(int p) { return p / N1 + N2 * (p % N1); }
-  __device__ __forceinline__ static int pos_of_freq(int k) { return k / N2 + N1 * (k % N2); }
+  PF_HD static int freq_of_pos(int p) { return p / N1 + N2 * (p % N1); }
+  PF_HD static int pos_of_freq(int k) { return k / N2 + N1 * (k % N2); }
 };
 
 // ---------------------------------------------------------------------------

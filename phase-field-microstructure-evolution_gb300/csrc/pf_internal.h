@@ -32,13 +32,15 @@ struct YZKernels {
 // default; the run-creation autotuner times the others.
 constexpr int kMaxVariants = 16;
 int x_variants_a(int nx, XKernels* out, int n);
+int x_variants_r5(int nx, XKernels* out, int n);
 int yz_variants_small(int ny, int nz, YZKernels* out, int n);
 int yz_variants_128a(int ny, int nz, YZKernels* out, int n);
 int yz_variants_128b(int ny, int nz, YZKernels* out, int n);
 int yz_variants_256a(int ny, int nz, YZKernels* out, int n);
 int yz_variants_256b(int ny, int nz, YZKernels* out, int n);
+int yz_variants_r5(int ny, int nz, YZKernels* out, int n);
 
-inline int get_x_variants(int nx, XKernels* out) { return x_variants_a(nx, out, 0); }
+inline int get_x_variants(int nx, XKernels* out) { return x_variants_r5(nx, out, x_variants_a(nx, out, 0)); }
 inline int get_yz_variants(int ny, int nz, YZKernels* out) {
   int n = 0;
   n = yz_variants_small(ny, nz, out, n);
@@ -46,6 +48,7 @@ inline int get_yz_variants(int ny, int nz, YZKernels* out) {
   n = yz_variants_128b(ny, nz, out, n);
   n = yz_variants_256a(ny, nz, out, n);
   n = yz_variants_256b(ny, nz, out, n);
+  n = yz_variants_r5(ny, nz, out, n);
   return n;
 }
 // default (first) variant of a shape; `out` receives one entry

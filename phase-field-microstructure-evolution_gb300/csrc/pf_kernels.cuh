@@ -524,7 +524,8 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
   using LM = Line<M>;
   constexpr int PM = LM::PITCH;
   constexpr int NP = LM::N2 / 2 + 1;  // run pairs per line
-  static_assert(LM::N2 % 2 == 0, "x plan needs an even number of runs");
+  // run pairs (pr, N2 - pr) for 0 < pr < N2/2, run 0 alone, and for even N2
+  // the run N2/2 paired with itself (x_inv_runs / x_fwd_runs)
   extern __shared__ float2 smem[];
   const RunParams& rp = runs[blockIdx.y];
   const int nF = (MODE == MODE_XJ) ? 1 : rp.V + 1;
@@ -1407,7 +1408,6 @@ __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restric
   constexpr int M = G::M, PM = G::PM, S = G::S;
   using LM = Line<M>;
   constexpr int NP = LM::N2 / 2 + 1;
-  static_assert(LM::N2 % 2 == 0, "x plan needs an even number of runs");
   enum { A_PRE = 0, A_N4, A_PAIRS, A_MABS, A_NN, A_PP, A_C };
   extern __shared__ float2 smem[];
   const RunParams& rp = runs[blockIdx.y];

@@ -2,7 +2,7 @@
 // sweeps such as tests/run_phase_sim.py and tests/scaling_tests.py submit
 // (one SLURM job per case there, run_phase_sim.py:130-172).
 //
-//   pf_sweep [--max-batch N] <case dir> [<case dir> ...]
+//   pf_sweep [--max-batch N] [--devices N|all] <case dir> [<case dir> ...]
 //
 // Every case directory holds an input.txt (the file run_phase_sim.py:112-128
 // writes) and receives what `var_diff.x <dir>/input.txt <dir>/` writes:
@@ -19,6 +19,11 @@
 // batched case holds the batch's step time.  Cases on the FP64 path (a grid
 // the fused kernels do not cover, or precision=64) run one at a time.
 //
+// --devices spreads the work units (batches and single cases) over N GPUs
+// (all: every visible one) with pf_place_units -- largest unit first onto the
+// device with the least work -- and runs each device's units in a thread of
+// its own.  Cases never exchange data, so there is no collective.
+//
 // Exit status: 0 if every case finished, 2 if a case failed to start or to
 // write, 3 if a case produced non-finite values (its records up to that step
 // are written; the other cases are unaffected).
@@ -29,6 +34,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -172,15 +178,32 @@ void run_batch(std::vector<Member*>& ms) {
 
 }  // namespace
 
+// a batch of same-class cases, or one FP64-path case
+struct Unit {
+  std::vector<Member*> ms;
+  bool single = false;
+  double work = 0;
+};
+
 int main(int argc, char** argv) {
-  int max_batch = 64;
+  int max_batch = 64, ndev = 1;
   std::vector<std::string> dirs;
   for (int i = 1; i < argc; ++i) {
-    if (!strcmp(argv[i], "--max-batch") && i + 1 < argc) max_batch = std::max(1, atoi(argv[++i]));
-    else dirs.push_back(argv[i]);
+    if (!strcmp(argv[i], "--max-batch") && i + 1 < argc) {
+      max_batch = std::max(1, atoi(argv[++i]));
+    } else if (!strcmp(argv[i], "--devices") && i + 1 < argc) {
+      ++i;
+      if (!strcmp(argv[i], "all")) {
+        ndev = std::max(1, pf_device_count());
+      } else {
+        ndev = std::max(1, atoi(argv[i]));
+      }
+    } else {
+      dirs.push_back(argv[i]);
+    }
   }
   if (dirs.empty()) {
-    fprintf(stderr, "usage: pf_sweep [--max-batch N] <case dir> [<case dir> ...]\n");
+    fprintf(stderr, "usage: pf_sweep [--max-batch N] [--devices N|all] <case dir> [<case dir> ...]\n");
     return 1;
   }
   std::vector<Member> ms(dirs.size());
@@ -215,23 +238,55 @@ int main(int argc, char** argv) {
       groups[std::make_tuple(c.in.Nx, c.in.Ny, c.in.Nz, c.in.var, varmob)].push_back(&m);
     }
   }
+  std::vector<Unit> units;
   size_t nbatches = 0;
   for (auto& kv : groups) {
     std::vector<Member*>& g = kv.second;
     for (size_t a = 0; a < g.size(); a += max_batch) {
-      std::vector<Member*> part(g.begin() + a, g.begin() + std::min(g.size(), a + (size_t)max_batch));
-      run_batch(part);
+      Unit u;
+      u.ms.assign(g.begin() + a, g.begin() + std::min(g.size(), a + (size_t)max_batch));
+      units.push_back(u);
       ++nbatches;
     }
   }
-  for (Member* m : singles) run_single(*m);
+  for (Member* m : singles) {
+    Unit u;
+    u.ms.push_back(m);
+    u.single = true;
+    units.push_back(u);
+  }
+  // a batch steps as long as its longest member
+  std::vector<double> work(units.size());
+  for (size_t u = 0; u < units.size(); ++u) {
+    int nmax = 0;
+    for (Member* m : units[u].ms) nmax = std::max(nmax, m->c->in.N_step);
+    for (Member* m : units[u].ms) units[u].work += pf_run_work(&m->c->cfg, nmax);
+    work[u] = units[u].work;
+  }
+  std::vector<int> dev(units.size(), 0);
+  pf_place_units(work.data(), (int)units.size(), ndev, dev.data(), nullptr);
+  auto run_device = [&](int d) {
+    for (size_t u = 0; u < units.size(); ++u) {
+      if (dev[u] != d) continue;
+      for (Member* m : units[u].ms) m->c->cfg.device = d;
+      if (units[u].single) run_single(*units[u].ms[0]);
+      else run_batch(units[u].ms);
+    }
+  };
+  if (ndev == 1) {
+    run_device(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int d = 0; d < ndev; ++d) th.emplace_back(run_device, d);
+    for (auto& t : th) t.join();
+  }
   int status = 0, ok = 0;
   for (Member& m : ms) {
     m.c->close();
     if (m.status == 0) ++ok;
     status = std::max(status, m.status);
   }
-  printf(" pf_sweep: %d of %zu cases finished (%zu batches, %zu FP64 cases)\n", ok, ms.size(), nbatches,
-         singles.size());
+  printf(" pf_sweep: %d of %zu cases finished (%zu batches, %zu FP64 cases, %d device%s)\n", ok, ms.size(), nbatches,
+         singles.size(), ndev, ndev == 1 ? "" : "s");
   return status;
 }

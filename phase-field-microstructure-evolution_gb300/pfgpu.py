@@ -29,7 +29,8 @@ EXPORTED = (
     "pf_ic_polycryst", "pf_insert_precipitates", "pf_format_e", "pf_format_summary", "pf_format_list_int",
     "pf_format_list_real", "pf_analyze_fields", "pf_analyze_run", "pf_write_vtk_real", "pf_write_vtk_int",
     "pf_server_create", "pf_server_submit", "pf_server_poll", "pf_server_wait", "pf_server_destroy",
-    "pf_server_last_error",
+    "pf_server_last_error", "pf_device_count", "pf_run_work", "pf_pick_device", "pf_place_units", "pf_pool_create", "pf_pool_devices",
+    "pf_pool_submit", "pf_pool_wait", "pf_pool_destroy", "pf_pool_last_error",
 )
 
 
@@ -93,6 +94,10 @@ class Input(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("max_active", C.c_int), ("hbm_budget_bytes", C.c_double),
                 ("chunk_steps", C.c_int), ("reserved", C.c_int * 5)]
+
+
+class PoolConfig(C.Structure):
+    _fields_ = [("ndevices", C.c_int), ("devices", C.POINTER(C.c_int)), ("server", ServerConfig)]
 
 
 class RequestTimes(C.Structure):
@@ -185,6 +190,16 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_server_wait": (C.c_int, [C.c_void_p, C.c_longlong, C.c_double, dp, dp, P(Diag), P(RequestTimes)]),
         "pf_server_destroy": (C.c_int, [C.c_void_p]),
         "pf_server_last_error": (C.c_char_p, []),
+        "pf_device_count": (C.c_int, []),
+        "pf_run_work": (C.c_double, [P(Config), C.c_int]),
+        "pf_pick_device": (C.c_int, [dp, C.c_int]),
+        "pf_place_units": (C.c_int, [dp, C.c_int, C.c_int, ip, dp]),
+        "pf_pool_create": (C.c_int, [P(PoolConfig), P(C.c_void_p)]),
+        "pf_pool_devices": (C.c_int, [C.c_void_p]),
+        "pf_pool_submit": (C.c_int, [C.c_void_p, P(Config), dp, dp, C.c_int, P(C.c_longlong), ip]),
+        "pf_pool_wait": (C.c_int, [C.c_void_p, C.c_longlong, C.c_double, dp, dp, P(Diag), P(RequestTimes)]),
+        "pf_pool_destroy": (C.c_int, [C.c_void_p]),
+        "pf_pool_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -632,6 +647,80 @@ class Server:
     def close(self):
         if getattr(self, "h", None):
             self.lib.pf_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# independent runs over the node's GPUs (placement only, no collective)
+# ---------------------------------------------------------------------------
+def place_units(work, ndev: int):
+    """LPT placement of work units on ndev devices (pf_place_units): returns
+    (device of each unit, work per device)."""
+    lib = load_library()
+    w = np.ascontiguousarray(work, dtype=np.float64)
+    dev = np.empty(len(w), dtype=np.int32)
+    load = np.empty(ndev, dtype=np.float64)
+    _check(lib.pf_place_units(_dp(w), len(w), ndev, dev.ctypes.data_as(C.POINTER(C.c_int)), _dp(load)))
+    return dev, load
+
+
+def pick_device(outstanding) -> int:
+    o = np.ascontiguousarray(outstanding, dtype=np.float64)
+    return load_library().pf_pick_device(_dp(o), len(o))
+
+
+class Pool:
+    """pf_pool: one pf_server per device, each run placed on the device with
+    the least outstanding work."""
+
+    def __init__(self, ndevices: int = 0, max_active: int = 0, hbm_budget_bytes: float = 0.0, chunk_steps: int = 0):
+        self.lib = load_library()
+        cfg = PoolConfig()
+        cfg.ndevices = ndevices
+        cfg.server.max_active, cfg.server.hbm_budget_bytes, cfg.server.chunk_steps = max_active, hbm_budget_bytes, \
+            chunk_steps
+        h = C.c_void_p()
+        rc = self.lib.pf_pool_create(C.byref(cfg), C.byref(h))
+        if rc != PF_OK:
+            raise PFError(rc, self.lib.pf_pool_last_error().decode())
+        self.h = h
+        self.devices = self.lib.pf_pool_devices(h)
+        self._shape = {}
+
+    def submit(self, params, phi: np.ndarray, con: np.ndarray, nsteps: int):
+        """Queue a run; returns (id, device ordinal)."""
+        cfg = make_config(params, PF_FP32_FUSED, 0)
+        a = to_aos(phi)
+        c = np.ascontiguousarray(con, dtype=np.float64)
+        rid, dev = C.c_longlong(), C.c_int()
+        rc = self.lib.pf_pool_submit(self.h, C.byref(cfg), _dp(a), _dp(c), int(nsteps), C.byref(rid), C.byref(dev))
+        if rc != PF_OK:
+            raise PFError(rc, self.lib.pf_pool_last_error().decode())
+        self._shape[rid.value] = (params.var, params.Nz, params.Ny, params.Nx)
+        return rid.value, dev.value
+
+    def wait(self, rid: int, timeout: float = -1.0):
+        var, nz, ny, nx = self._shape.pop(rid)
+        a = np.empty((nz, ny, nx, var))
+        c = np.empty((nz, ny, nx))
+        d = Diag()
+        t = RequestTimes()
+        rc = self.lib.pf_pool_wait(self.h, rid, timeout, _dp(a), _dp(c), C.byref(d), C.byref(t))
+        if rc == PF_EBUSY:
+            self._shape[rid] = (var, nz, ny, nx)
+        if rc != PF_OK:
+            raise PFError(rc, self.lib.pf_pool_last_error().decode())
+        return from_aos(a), c, d.as_dict(), {k: getattr(t, k) for k, _ in t._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pf_pool_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -170,3 +170,22 @@ def test_driver_fp64_path_for_other_grids(pkg, oracle, tmp_path):
     for s in want_rows:
         for g, w in zip(got[s], want_rows[s]):
             assert abs(g - w) <= 5e-7 * abs(w) + 1e-12
+
+
+def test_driver_weak_scaling_grid_80_baseline(pkg, oracle, tmp_path):
+    """One of the reference's weak-scaling grids (80^3, inputs/config.yaml:76-79)
+    with its baseline coefficients (var 55, dt 1e-4, am 0.5, ap 5, c0 0.1 / 1,
+    d_gb 1) runs on the fused FP32 path and matches the oracle."""
+    exe = str(pkg.driver_path())
+    kw = dict(Nx=80, Ny=80, Nz=80, var=55, t_step=1e-4, am=0.5, ap=5.0, con_0_mat=0.1, con_0_ppt=1.0)
+    inp = canonical_input(tmp_path / "input.txt", N_step=4, ifreq=4, ppt_int=0, grn_rad=10, num_ppt=6,
+                          c_mat=0.5, c_ppt=0.5, d_gb=1.0, ijk_ppt=(40, 40, 40), **kw)
+    r = _run(exe, inp, tmp_path, str(tmp_path) + "/")
+    assert "fused FP32" in r.stdout, r.stdout
+    p = _params(oracle, D_gb=1.0, **kw)
+    gen = oracle.Ran2()
+    phi, con, idum = oracle.ic_circle(p, 10, (2, 2, 2), 6, -1, 0.5, 1.0, gen=gen)
+    want_rows, want = _oracle_protocol(oracle, p, (phi, con, idum, gen), 4)
+    _check_rows(_summary(tmp_path / "summary.dat"), want_rows, p)
+    gphi, gcon = pkg.read_data_save(tmp_path / "step_0000004" / "data_save.0001", p)
+    assert np.max(np.abs(gphi - want[4][0])) < TOL and np.max(np.abs(gcon - want[4][1])) < TOL

@@ -102,3 +102,25 @@ def test_server_long_chunks_keep_their_records(pkg, oracle):
     run.close()
     assert np.array_equal(gp, ap) and np.array_equal(gc, ac)
     assert last == d[-1], (last, d[-1])
+
+
+def test_pool_over_visible_devices_equals_runs_alone(pkg, oracle):
+    """pf_pool: one server per visible GPU, every request placed on the device
+    with the least outstanding work; results equal the runs alone."""
+    reqs = _requests(oracle)[:4]
+    pool = pkg.Pool(max_active=8, chunk_steps=32)
+    try:
+        assert pool.devices == pkg.load_library().pf_device_count() >= 1
+        subs = [pool.submit(p, phi, con, steps) for p, phi, con, steps, _ in reqs]
+        assert all(0 <= d < pool.devices for _, d in subs)
+        results = [pool.wait(i, timeout=600.0) for i, _ in subs]
+    finally:
+        pool.close()
+    for (p, phi, con, steps, _), (gp, gc, last, _) in zip(reqs, results):
+        run = pkg.Run(p)
+        run.set_fields(phi, con)
+        d = run.step(steps)
+        ap, ac = run.get_fields()
+        run.close()
+        assert np.array_equal(gp, ap) and np.array_equal(gc, ac)
+        assert last == d[-1]

@@ -46,10 +46,13 @@ def _cases(oracle, root):
     return dirs
 
 
-def test_sweep_equals_single_runs(pkg, oracle, tmp_path):
+@pytest.mark.parametrize("devices", [None, "all"])
+def test_sweep_equals_single_runs(pkg, oracle, tmp_path, devices):
+    """devices "all": the work units placed over every visible GPU."""
     env = dict(os.environ, PFGPU_AUTOTUNE="0")  # the same kernel variants in both processes
     dirs = _cases(oracle, tmp_path)
-    r = subprocess.run([str(pkg.sweep_path()), "--max-batch", "2"] + [str(v["sweep"]) for v in dirs.values()],
+    extra = ["--devices", devices] if devices else []
+    r = subprocess.run([str(pkg.sweep_path()), "--max-batch", "2"] + extra + [str(v["sweep"]) for v in dirs.values()],
                        capture_output=True, text=True, timeout=900, env=env)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "5 of 5 cases finished" in r.stdout and "1 FP64 cases" in r.stdout

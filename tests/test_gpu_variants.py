@@ -11,7 +11,10 @@ from test_gpu_parity import TOL32, _check_diag, _check_fields
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(32, 32, 32, 5), (64, 64, 64, 4), (96, 96, 96, 3), (128, 128, 128, 3), (64, 32, 64, 3)]
+# (the factor-5 grids 80^3 and 160^3 are the reference's weak-scaling grids,
+# inputs/config.yaml:71-106)
+SHAPES = [(32, 32, 32, 5), (64, 64, 64, 4), (96, 96, 96, 3), (128, 128, 128, 3), (64, 32, 64, 3), (80, 80, 80, 4),
+          (160, 160, 160, 3)]
 
 
 def _run(pkg, p, phi, con, steps, env):
@@ -56,19 +59,21 @@ def test_every_variant_matches_oracle(pkg, oracle, shape):
     assert len(seen) >= nxv  # every x variant ran (a yz variant that cannot be scheduled falls back)
 
 
-def test_every_variant_256(pkg, oracle):
-    """256^3: each variant against the FP64 GPU path (the oracle would take
-    minutes per step at this size), with 17 fields so that every x variant's
-    per-warp reductions are exercised."""
-    p = oracle.Params(256, 256, 256, 16, t_step=0.02, am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7)
-    phi, con = oracle.ic_voronoi(p, 2, 24, 0.01, 0.4, 0.02)
+@pytest.mark.parametrize("n,var", [(256, 16), (200, 8)])
+def test_every_variant_large(pkg, oracle, n, var):
+    """256^3 and 200^3 (the largest of the reference's weak-scaling grids):
+    each variant against the FP64 GPU path (the oracle would take minutes per
+    step at this size), with enough fields that every x variant's per-warp
+    reductions are exercised."""
+    p = oracle.Params(n, n, n, var, t_step=0.02, am=0.5, ap=2.0, con_0_mat=0.3, con_0_ppt=0.7)
+    phi, con = pkg.ic_voronoi(p, 2, 24, 0.01, 0.4, 0.02)
     steps = 2
     run = pkg.Run(p, precision=pkg.PF_FP64_PLAIN)
     run.set_fields(phi, con)
     hd = run.step(steps)
     hp, hc = run.get_fields()
     run.close()
-    nxv, nyzv = pkg.variant_counts(256, 256, 256)
+    nxv, nyzv = pkg.variant_counts(n, n, n)
     envs = [{"PFGPU_X_VARIANT": str(i), "PFGPU_YZ_VARIANT": "0"} for i in range(nxv)]
     envs += [{"PFGPU_X_VARIANT": "0", "PFGPU_YZ_VARIANT": str(j)} for j in range(1, nyzv)]
     for env in envs:
