@@ -422,6 +422,11 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Voronoi polycrystal from the ran_2 stream, no dataset)",
+            "timing": {"repeats": len(rep_ms), "steps_per_repeat": args.steps,
+                       "ms_per_repeat_median": statistics.median(rep_ms),
+                       "ms_per_repeat_min": min(rep_ms), "ms_per_repeat_max": max(rep_ms),
+                       "what": "value and ms_per_step from the median repeat of K steps (CUDA events on the "
+                               "library's stream); repeats continue until at least %.1f s" % args.min_timed_s},
             "config": {"workload": WORKLOAD_NAME, "grid": [p.Nx, p.Ny, p.Nz], "P": p.var, "runs_per_gpu": 1,
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single run",
                        "l2": "inputs larger than L2: %.0f MB resident state + scratch per step > 129 MB L2" %

@@ -2,6 +2,8 @@
 // construction, CUDA-graph step driver and host<->device field transfer for
 // the fused FP32 path.  The FP64 plain path and the Fortran shims live in
 // pf_plain64.cu, the host-side RNG in pf_host.cpp.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder is fetched through the runtime)
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -145,6 +147,40 @@ static size_t x_smem(int nx, int nF, int wy) {
 }
 
 static const size_t kMaxSmem = 227 * 1024;
+
+// cuTensorMapEncodeTiled through the runtime's driver entry points (no link
+// against the driver library).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// Tensor map over a run's mixed-space state Sm [nF][Kx][Nz][Ny] (8-byte
+// complex elements) with box {wy rows, 1 z, Kx, 1 field}: one TMA copy brings
+// the half spectra of wy rows of one field at one z.
+static int encode_sm_map(void* Sm, int Ny, int Nz, int Kx, int nF, int wy, CUtensorMap* out) {
+  const PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
+  if (!fn) return fail(PF_ECUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const cuuint64_t dims[4] = {(cuuint64_t)Ny, (cuuint64_t)Nz, (cuuint64_t)Kx, (cuuint64_t)nF};
+  const cuuint64_t strides[3] = {(cuuint64_t)Ny * 8, (cuuint64_t)Ny * Nz * 8, (cuuint64_t)Kx * Ny * Nz * 8};
+  const cuuint32_t box[4] = {(cuuint32_t)wy, 1, (cuuint32_t)Kx, 1};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  const CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, Sm, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PF_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return PF_OK;
+}
 // order parameters per run; the x pass must also fit (var+1) field lines of
 // its rows in shared memory (checked below)
 static const int kMaxVar = 255;
@@ -191,6 +227,7 @@ struct pf_batch {
   YZKernels yk{};
   size_t smem_x = 0, smem_xj = 0, smem_bulk = 0;
   std::vector<RunParams> hrp;
+  std::vector<CUtensorMap> tmaps;  // host copies of the runs' tensor maps (TMA x pass)
   RunParams* drp = nullptr;
   void* mem = nullptr;         // all per-run buffers
   float* fin = nullptr;        // float staging [nF][Nz][Ny][Nx]
@@ -202,6 +239,7 @@ struct pf_batch {
   cudaStream_t copy = nullptr;        // record copies of completed steps (never waits for later steps)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int prio_hi = 0;                    // greatest stream priority of the device
+  int nsm = 0;                        // multiprocessors of the device (persistent TMA x pass)
   std::vector<double> hdiag;
   std::vector<int> steps_done;
   std::string variant;  // chosen kernel variants, for reports
@@ -258,6 +296,12 @@ static int launch_xj(pf_batch* b, cudaStream_t s, int prio = 0) {
 static int launch_x_bulk(pf_batch* b, cudaStream_t s) {
   const int R = b->nruns;
   const unsigned nblk = (unsigned)(b->Nz * (b->Ny / b->xk.wy));
+  if (b->xk.tma) {  // persistent: about one CTA per SM over all runs
+    const unsigned g = (unsigned)std::max(1, std::min((int)nblk, b->nsm / R));
+    b->xk.bulk<<<dim3(g, R), b->xk.threads, b->smem_bulk, s>>>(b->drp, b->tab.sh);
+    PF_CUDA(cudaGetLastError());
+    return PF_OK;
+  }
   if (!b->xk.cl) {
     b->xk.bulk<<<dim3(nblk, R), b->xk.threads, b->smem_bulk, s>>>(b->drp, b->tab.sh);
     PF_CUDA(cudaGetLastError());
@@ -384,6 +428,14 @@ static bool x_ok(pf_batch* b, const XKernels& k) {
   if (b->Ny % k.wy != 0) return false;
   const size_t sm = x_smem(b->Nx, b->nF, k.wy);
   if (sm > kMaxSmem) return false;
+  if (k.tma) {  // persistent TMA bulk kernel: staging + lines must fit one CTA; inner TMA box of 16-byte multiples
+    const size_t sb = k.bulk_smem(b->nF);
+    CUtensorMap probe;
+    if (sb > kMaxSmem || (k.wy * 8) % 16 != 0 || b->Kx > 256 ||
+        encode_sm_map(b->hrp[0].Sm, b->Ny, b->Nz, b->Kx, b->nF, k.wy, &probe) != PF_OK ||
+        !raise_smem((const void*)k.bulk, sb))
+      return false;
+  }
   if (k.cl) {  // two-CTA bulk: rank 1 must own phi_P and c (var >= 3); the cluster must be schedulable
     const size_t sb = k.bulk_smem(b->nF);
     if (b->V < 3 || sb > kMaxSmem || !raise_smem((const void*)k.bulk, sb)) return false;
@@ -405,7 +457,7 @@ static bool x_ok(pf_batch* b, const XKernels& k) {
     }
   }
   for (KernelFn f : {k.bulk, k.xj, k.imp, k.exp}) {
-    if (k.cl && f == k.bulk) continue;
+    if ((k.cl || k.tma) && f == k.bulk) continue;
     if (!raise_smem((const void*)f, sm)) return false;
   }
   return true;
@@ -421,7 +473,8 @@ static bool xj_ok(pf_batch* b, const XKernels& k) {
 static void describe_variants(pf_batch* b) {
   char buf[160];
   snprintf(buf, sizeof buf, "x:wy=%d,threads=%d%s yz:cluster=%d,threads=%d xj:wy=%d,threads=%d", b->xk.wy,
-           b->xk.threads, b->xk.cl ? ",cluster=2" : "", b->yk.cluster, b->yk.threads, b->xjk.wy, b->xjk.threads);
+           b->xk.threads, b->xk.cl ? ",cluster=2" : (b->xk.tma ? ",tma" : ""), b->yk.cluster, b->yk.threads,
+           b->xjk.wy, b->xjk.threads);
   b->variant = buf;
 }
 
@@ -431,11 +484,27 @@ static void apply_xj(pf_batch* b, const XKernels& k) {
   describe_variants(b);
 }
 
+// Tensor maps of every run for the TMA x pass with wy rows per tile, written
+// on the batch's stream (in order with the launches that read them).
+static int write_tensor_maps(pf_batch* b, int wy) {
+  for (int r = 0; r < b->nruns; ++r) {
+    CUtensorMap m;
+    const int rc = encode_sm_map(b->hrp[r].Sm, b->Ny, b->Nz, b->Kx, b->nF, wy, &m);
+    if (rc) return rc;
+    b->tmaps[r] = m;
+  }
+  for (int r = 0; r < b->nruns; ++r)
+    PF_CUDA(cudaMemcpyAsync(const_cast<void*>(b->hrp[r].tmap_sm), &b->tmaps[r], sizeof(CUtensorMap),
+                            cudaMemcpyHostToDevice, b->stream));
+  return PF_OK;
+}
+
 static void apply_variants(pf_batch* b, const XKernels& xk, const YZKernels& yk) {
   b->xk = xk;
   b->yk = yk;
   b->smem_x = x_smem(b->Nx, b->nF, xk.wy);
-  b->smem_bulk = xk.cl ? xk.bulk_smem(b->nF) : b->smem_x;
+  b->smem_bulk = (xk.cl || xk.tma) ? xk.bulk_smem(b->nF) : b->smem_x;
+  if (xk.tma) write_tensor_maps(b, xk.wy);  // encodable: checked by x_ok
   b->tab.sh.nblk_x = b->Nz * (b->Ny / xk.wy);
   b->tab.sh.nblk_yz = yk.cluster * b->nF * b->Kx;
   apply_xj(b, xk);
@@ -542,7 +611,7 @@ static int tune_batch(pf_batch* b) {
         PF_CUDA(cudaMemsetAsync(r.Sk, 0, fbytes, b->stream));
         PF_CUDA(cudaMemsetAsync(r.Sm, 0, fbytes, b->stream));
         PF_CUDA(cudaMemsetAsync(r.D, 0, fbytes, b->stream));
-        PF_CUDA(cudaMemsetAsync(r.counter, 0, 128, b->stream));  // step counter and ticket
+        PF_CUDA(cudaMemsetAsync(r.counter, 0, 256, b->stream));  // step counter, ticket, error word
       }
       PF_CUDA(cudaStreamSynchronize(b->stream));
       g_tune_cache[key] = std::make_tuple(bx, by, bj);
@@ -623,8 +692,9 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   const size_t szPx = align((size_t)XD_COUNT * b->Nz * b->Ny * sizeof(double));
   const size_t szPyz = align((size_t)16 * b->nF * b->Kx * sizeof(double));
   const size_t szDiag = align((size_t)b->ring * DR_COUNT * sizeof(double));
-  const size_t szCnt = 256;
-  const size_t per_run = 3 * szS + szMob + szJ + szPx + szPyz + szDiag + szCnt;
+  const size_t szCnt = 256;   // step counter, ticket, error word (one 64-byte line each)
+  const size_t szTmap = 256;  // TMA tensor map of Sm (128 bytes, 64-byte aligned)
+  const size_t per_run = 3 * szS + szMob + szJ + szPx + szPyz + szDiag + szCnt + szTmap;
   e = cudaMalloc(&b->mem, per_run * nruns);
   if (e != cudaSuccess)
     return bail(fail(PF_ENOMEM, "cudaMalloc(%zu bytes) for %d runs: %s", per_run * nruns, nruns, cudaGetErrorString(e)));
@@ -635,7 +705,10 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   e = cudaMalloc(&b->dstage, b->nF * ncell * sizeof(double));
   if (e != cudaSuccess) return bail(fail(PF_ENOMEM, "staging allocation: %s", cudaGetErrorString(e)));
   b->hrp.resize(nruns);
+  b->tmaps.resize(nruns);
   b->steps_done.assign(nruns, 0);
+  cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, b->device);
+  if (b->nsm < 1) b->nsm = 1;
   for (int i = 0; i < nruns; ++i) {
     const pf_config& c = cfgs[i];
     char* p = (char*)b->mem + per_run * i;
@@ -646,11 +719,14 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
     r.D = (float2*)p; p += szS;
     r.mob = var ? (float*)p : nullptr; p += szMob;
     r.J = var ? (float2*)p : nullptr; p += szJ;
-    r.part_x = (double*)p; p += szPx;
-    r.part_yz = (double*)p; p += szPyz;
+    r.part_x = (float*)p; p += szPx;
+    r.part_yz = (float*)p; p += szPyz;
     r.diag = (double*)p; p += szDiag;
     r.counter = (int*)p;
     r.ticket = (unsigned*)(p + 64);  // own 64-byte line in the 256-byte counter block
+    r.err = (unsigned*)(p + 128);
+    p += szCnt;
+    r.tmap_sm = p;
     r.fin = b->fin;
     r.L = (float)c.mob_phi;
     r.kappa_phi = (float)c.grad_coeff_phi;
@@ -713,7 +789,7 @@ static int batch_set_fields(pf_batch* b, int run, const double* phi, const doubl
   b->xk.imp<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
   int rc = launch_yz(b, b->yk.imp, b->nF * b->Kx, b->drp + run, 1, b->stream);
   if (rc) return rc;
-  PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, 128, b->stream));  // step counter and ticket
+  PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, 256, b->stream));  // step counter, ticket, error word
   PF_CUDA(cudaGetLastError());
   PF_CUDA(cudaStreamSynchronize(b->stream));
   b->steps_done[run] = 0;
@@ -907,7 +983,7 @@ size_t pf_batch_bytes(const pf_config* c, int nruns) {
   const bool var = c->mobility == PF_MOB_C1MC || c->D_gb != 0.0;
   auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const size_t per_run = 3 * align(nF * fieldc * 8) + (var ? align(ncell * 4) + align(fieldc * 8) : 0) +
-                         align((size_t)XD_COUNT * plane * 8) + align(16 * nF * Kx * 8) + align(1024 * DR_COUNT * 8) + 256;
+                         align((size_t)XD_COUNT * plane * 8) + align(16 * nF * Kx * 8) + align(1024 * DR_COUNT * 8) + 512;
   return per_run * nruns + nF * ncell * 12 + ((size_t)1 << 20);
 }
 // Steps run `run` has completed since its last set_fields (host count).

@@ -35,8 +35,15 @@ namespace cg = cooperative_groups;
 
 namespace pf {
 
-// Number of per-block diagnostic partials written by the x pass.
-enum XDiag { XD_FETA = 0, XD_FCH, XD_MASS, XD_CMIN, XD_CMAX, XD_PHIMIN, XD_PHIPMAX, XD_NONFINITE, XD_COUNT };
+// Per-block diagnostic partials of the x pass (floats; the sums as
+// compensated hi + lo pairs): part_x[q * nblk_x + block].
+enum XDiag {
+  XQ_FETA_H = 0, XQ_FETA_L, XQ_FCH_H, XQ_FCH_L, XQ_MASS_H, XQ_MASS_L,
+  XQ_CMIN, XQ_CMAX, XQ_PHIMIN, XQ_PHIPMAX, XQ_BAD, XQ_COUNT
+};
+// room reserved per (z, y) row for the x partials (doubles' worth, any variant)
+constexpr int XD_COUNT = 8;
+static_assert(XQ_COUNT * 4 <= XD_COUNT * 8, "x partials must fit the reserved room");
 // Per-step diagnostic record layout (doubles)
 enum DiagRec {
   DR_STEP = 0, DR_FINT, DR_FETA, DR_FCH, DR_CMIN, DR_CMAX, DR_PHIMIN, DR_PHIPMAX, DR_MASS, DR_NONFINITE, DR_COUNT
@@ -52,11 +59,13 @@ struct RunParams {
   float2* D;       // [nF][Kx][Nz][Ny] x-spectra of dF/dphi_i and dF/dc
   float* mob;      // [Nz][Ny][Nx] mobility minus D_mean (variable mobility only)
   float2* J;       // [Kx][Nz][Ny] CH flux scratch (variable mobility only)
-  double* part_x;  // [XD_COUNT][nblk_x]
-  double* part_yz; // [nblk_yz]
+  float* part_x;   // [XQ_COUNT][nblk_x]
+  float* part_yz;  // [2][nblk_yz]: hi and lo of each yz CTA's weighted f_int sum
   double* diag;    // [ring][DR_COUNT]
   int* counter;    // step counter (device)
   unsigned* ticket;  // CTAs of the step's yz pass that have finished (reset by the last one)
+  unsigned* err;     // bit 0: a TMA tile of the x pass never arrived (the step's record is flagged)
+  const void* tmap_sm;  // TMA tensor map over Sm [nF][Kx][Nz][Ny] (x pass TMA variant), global memory
   float* fin;      // [nF][Nz][Ny][Nx] real fields for import/export
   float L, kappa_phi, kappa_c, dt, D_L, D_gb, sigma1, sigma2, am, ap, c0m, c0p;
   int mobility;
@@ -119,18 +128,25 @@ struct FF {
     hi = s;
     lo = __fadd_rn(lo, e);
   }
-};
-// sum of the pairs of a warp (every lane gets the same value)
-__device__ __forceinline__ double warp_sum_ff(FF x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float bh = __shfl_xor_sync(0xffffffffu, x.hi, o), bl = __shfl_xor_sync(0xffffffffu, x.lo, o);
+  __device__ __forceinline__ void add(const FF& o) {
     float s, e;
-    two_sum(x.hi, bh, s, e);
-    x.hi = s;
-    x.lo = __fadd_rn(__fadd_rn(x.lo, bl), e);
+    two_sum(hi, o.hi, s, e);
+    hi = s;
+    lo = __fadd_rn(__fadd_rn(lo, o.lo), e);
   }
-  return (double)x.hi + (double)x.lo;
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ FF ff(float hi, float lo = 0.f) {
+  FF x;
+  x.hi = hi;
+  x.lo = lo;
+  return x;
+}
+// sum of the pairs of a warp (every lane gets a sum of all 32)
+__device__ __forceinline__ FF warp_sum_ff(FF x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x.add(ff(__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)));
+  return x;
 }
 // compensated FP64 sum (Kahan-Babuska-Neumaier, the error of each addition
 // taken exactly by TwoSum): value() = s + c
@@ -216,10 +232,19 @@ __device__ __forceinline__ void passA_rt(float2* buf, int NL, const float2* __re
   }
 }
 
+// Element k of a half spectrum at src + k * stride: read-only global memory
+// (SMEM = false) or a shared-memory staging buffer (SMEM = true).
+template <bool SMEM>
+__device__ __forceinline__ float2 ld_spec(const float2* p) {
+  if constexpr (SMEM) return *p;
+  else return __ldg(p);
+}
+
 // Inverse x transform, first half: read the half spectrum of line (f, yy)
-// from global for the run pair `pr`, pre-process, inverse DFT_N1 of each run,
-// store the runs (pass B' output) into the padded line.
-template <int M>
+// (element kx at src + kx * plane) for the run pair `pr`, pre-process,
+// inverse DFT_N1 of each run, store the runs (pass B' output) into the padded
+// line.
+template <int M, bool SMEM = false>
 __device__ __forceinline__ void x_inv_runs(const float2* __restrict__ src, size_t plane, float2* line, int pr,
                                            const float2* __restrict__ twN) {
   constexpr int N1 = Line<M>::N1, N2 = Line<M>::N2;
@@ -228,8 +253,8 @@ __device__ __forceinline__ void x_inv_runs(const float2* __restrict__ src, size_
     float2 a[N1], b[N1];
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) {
-      a[k1] = __ldg(src + (size_t)(ra + N2 * k1) * plane);
-      b[k1] = __ldg(src + (size_t)(rb + N2 * k1) * plane);
+      a[k1] = ld_spec<SMEM>(src + (size_t)(ra + N2 * k1) * plane);
+      b[k1] = ld_spec<SMEM>(src + (size_t)(rb + N2 * k1) * plane);
     }
     float2 za[N1], zb[N1];
 #pragma unroll
@@ -247,8 +272,8 @@ __device__ __forceinline__ void x_inv_runs(const float2* __restrict__ src, size_
   } else if (pr == 0) {
     float2 a[N1];
 #pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) a[k1] = __ldg(src + (size_t)(N2 * k1) * plane);
-    const float2 xM = __ldg(src + (size_t)M * plane);
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = ld_spec<SMEM>(src + (size_t)(N2 * k1) * plane);
+    const float2 xM = ld_spec<SMEM>(src + (size_t)M * plane);
     float2 z[N1];
     z[0] = make_float2(a[0].x + xM.x, a[0].x - xM.x);
 #pragma unroll
@@ -266,7 +291,7 @@ __device__ __forceinline__ void x_inv_runs(const float2* __restrict__ src, size_
     const int ra = N2 / 2;
     float2 a[N1];
 #pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) a[k1] = __ldg(src + (size_t)(ra + N2 * k1) * plane);
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = ld_spec<SMEM>(src + (size_t)(ra + N2 * k1) * plane);
     float2 z[N1];
 #pragma unroll
     for (int k1 = 0; k1 < N1 / 2; ++k1) {
@@ -470,45 +495,119 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
 }
 
 // Block reduction of the x pass's diagnostics into the block's partials
-// part_x[q * nblk_x + blk] (all threads of the block call it).
+// part_x[q * nblk_x + blk] (all threads of the block call it).  Sums travel as
+// compensated FP32 pairs: FP64 arithmetic is scarce on this part, and a
+// serial FP64 chain at the end of every block held its shared memory (and
+// the next block) back.
 template <int T>
 __device__ __forceinline__ void store_block_diag(const BulkAcc& acc, const RunParams& rp, const Shape& sh, int blk) {
   static_assert(T % 32 == 0 && T <= 1024, "whole warps");
-  __shared__ double red_d[3][T / 32];  // one slot per warp
-  __shared__ float red_f[4][T / 32];
-  __shared__ int red_i[T / 32];
+  constexpr int NW = T / 32;
+  __shared__ float red_s[6][NW];  // hi, lo of f_eta, f_ch, mass per warp
+  __shared__ float red_m[4][NW];
+  __shared__ int red_i[NW];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const double s0 = warp_sum((double)acc.feta), s1 = warp_sum((double)acc.fch), s2 = warp_sum_ff(acc.mass);
+  const FF s0 = warp_sum_ff(ff(acc.feta)), s1 = warp_sum_ff(ff(acc.fch)), s2 = warp_sum_ff(acc.mass);
   const float m0 = warp_min(acc.cmin), m1 = warp_max(acc.cmax), m2 = warp_min(acc.phimin), m3 = warp_max(acc.phipmax);
   const int nb = __reduce_add_sync(0xffffffffu, acc.nonfinite);
   if (lane == 0) {
-    red_d[0][wid] = s0; red_d[1][wid] = s1; red_d[2][wid] = s2;
-    red_f[0][wid] = m0; red_f[1][wid] = m1; red_f[2][wid] = m2; red_f[3][wid] = m3;
+    red_s[0][wid] = s0.hi; red_s[1][wid] = s0.lo; red_s[2][wid] = s1.hi; red_s[3][wid] = s1.lo;
+    red_s[4][wid] = s2.hi; red_s[5][wid] = s2.lo;
+    red_m[0][wid] = m0; red_m[1][wid] = m1; red_m[2][wid] = m2; red_m[3][wid] = m3;
     red_i[wid] = nb;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double a0 = 0, a1 = 0;
-    KSum a2;
-    float b0 = red_f[0][0], b1 = red_f[1][0], b2 = red_f[2][0], b3 = red_f[3][0];
-    int nn = 0;
-    for (int w = 0; w < T / 32; ++w) {
-      a0 += red_d[0][w]; a1 += red_d[1][w]; a2.add(red_d[2][w]);
-      b0 = fminf(b0, red_f[0][w]); b1 = fmaxf(b1, red_f[1][w]);
-      b2 = fminf(b2, red_f[2][w]); b3 = fmaxf(b3, red_f[3][w]);
-      nn += red_i[w];
+  if (wid == 0) {  // the warps' values, one per lane (the reference's start values as identities)
+    const bool in = lane < NW;
+    const FF a0 = warp_sum_ff(in ? ff(red_s[0][lane], red_s[1][lane]) : ff(0.f));
+    const FF a1 = warp_sum_ff(in ? ff(red_s[2][lane], red_s[3][lane]) : ff(0.f));
+    const FF a2 = warp_sum_ff(in ? ff(red_s[4][lane], red_s[5][lane]) : ff(0.f));
+    const float b0 = warp_min(in ? red_m[0][lane] : 1.f), b1 = warp_max(in ? red_m[1][lane] : 0.f);
+    const float b2 = warp_min(in ? red_m[2][lane] : 1.f), b3 = warp_max(in ? red_m[3][lane] : 0.f);
+    const int nn = __reduce_add_sync(0xffffffffu, in ? red_i[lane] : 0);
+    if (lane == 0) {
+      const int nbk = sh.nblk_x;
+      float* p = rp.part_x + blk;
+      p[XQ_FETA_H * nbk] = a0.hi; p[XQ_FETA_L * nbk] = a0.lo;
+      p[XQ_FCH_H * nbk] = a1.hi;  p[XQ_FCH_L * nbk] = a1.lo;
+      p[XQ_MASS_H * nbk] = a2.hi; p[XQ_MASS_L * nbk] = a2.lo;
+      p[XQ_CMIN * nbk] = b0;
+      p[XQ_CMAX * nbk] = b1;
+      p[XQ_PHIMIN * nbk] = b2;
+      p[XQ_PHIPMAX * nbk] = b3;
+      p[XQ_BAD * nbk] = (float)nn;
     }
-    const int nbk = sh.nblk_x;
-    double* p = rp.part_x + blk;
-    p[XD_FETA * nbk] = a0;
-    p[XD_FCH * nbk] = a1;
-    p[XD_MASS * nbk] = a2.value();
-    p[XD_CMIN * nbk] = b0;
-    p[XD_CMAX * nbk] = b1;
-    p[XD_PHIMIN * nbk] = b2;
-    p[XD_PHIPMAX * nbk] = b3;
-    p[XD_NONFINITE * nbk] = nn;
   }
+}
+
+// Bulk terms of one tile (WY rows of every field in shared memory), one
+// float2 slot (two cells) per item.  Consecutive lanes take consecutive
+// physical slots of the padded lines and the pad slots stay idle, so that the
+// 16 slots of a half warp always fall in distinct bank pairs (a walk over the
+// logical cells would span 17 slots and put its first and last in one pair).
+template <int NX, int WY, int T>
+__device__ __forceinline__ void bulk_tile(float2* smem, const RunParams& rp, const Shape& sh, int z, int y0,
+                                          BulkAcc& acc) {
+  constexpr int M = NX / 2;
+  using LM = Line<M>;
+  constexpr int PM = LM::PITCH, N1 = LM::N1;
+  for (int it = threadIdx.x; it < WY * PM; it += T) {
+    const int yy = it / PM, ps = it - yy * PM;
+    const int q = ps / (N1 + 1), r = ps - q * (N1 + 1);
+    if (r == N1 || ps >= LM::RAW) continue;  // pad slot
+    const int m = q * N1 + r;
+    float2 dfdc, mob;
+    bulk_slot<PM, WY>(smem, yy, ps, rp, dfdc, mob, acc);
+    smem[(rp.V * WY + yy) * PM + ps] = dfdc;
+    if (rp.mobility != MOB_CONST)
+      *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = mob;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TMA (cp.async.bulk.tensor) and mbarrier helpers.  Tensor maps live in
+// global memory (one per run, written by the host before the launch); every
+// copy is a plain tile load from this GPU's own memory (no multicast).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// Wait for the phase of the given parity to complete, for at most about one
+// second of the global timer: false if it never completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+  uint64_t t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    uint64_t t1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+    if (t1 - t0 > 1000000000ull) return false;
+  }
+}
+// 4-D tile load of the box at coordinates (c0 innermost .. c3) into dst,
+// completing on bar.  c0 * element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+      "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"((uint32_t)__cvta_generic_to_shared(bar))
+      : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -572,15 +671,7 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
 
   if (MODE == MODE_BULK) {
     // 2. bulk terms, two cells per slot
-    for (int it = threadIdx.x; it < WY * M; it += T) {
-      const int m = it % M, yy = it / M;
-      const int slot = LM::phys(m);
-      float2 dfdc, mob;
-      bulk_slot<PM, WY>(smem, yy, slot, rp, dfdc, mob, acc);
-      smem[(rp.V * WY + yy) * PM + slot] = dfdc;
-      if (rp.mobility != MOB_CONST)
-        *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = mob;
-    }
+    bulk_tile<NX, WY, T>(smem, rp, sh, z, y0, acc);
     __syncthreads();
   } else if (MODE == MODE_XJ) {
     for (int it = threadIdx.x; it < WY * M; it += T) {
@@ -610,6 +701,99 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
 
   // 6. diagnostics: block reduction into per-block partials
   store_block_diag<T>(acc, rp, sh, blockIdx.x);
+}
+
+
+// ---------------------------------------------------------------------------
+// x pass (bulk mode) with TMA-staged loads, persistent over tiles.
+//
+// Each CTA owns one SM and walks the tiles (WY rows at one z, all fields)
+// tile = blockIdx.x, blockIdx.x + gridDim.x, ...  The mixed-space half spectra
+// of a tile arrive by TMA -- one box {WY rows, 1 z, Kx, 1 field} per field of
+// the run's tensor map over Sm [nF][Kx][Nz][Ny] -- into a staging buffer
+// [field][kx][row]; as soon as the inverse x transform has consumed them,
+// one thread issues the next tile's boxes, which land while the CTA runs the
+// rest of this tile (inverse pass A, bulk terms, forward transform, stores of
+// D and diagnostics).  The HBM latency that stalls the plain kernel's loads
+// thus overlaps the previous tile's arithmetic.  Results are identical to the
+// plain kernel's (same arithmetic, same per-tile partials).
+// ---------------------------------------------------------------------------
+template <int NX, int WY>
+struct XTMA {
+  static constexpr int M = NX / 2, KX = M + 1, PM = Line<M>::PITCH;
+  // staging of one field, a multiple of 128 bytes so that every TMA
+  // destination starts on a 128-byte boundary
+  static constexpr int FSTRIDE = ((KX * WY * 8 + 127) / 128) * 16;  // float2 elements
+  static constexpr size_t stage_bytes(int nF) { return (size_t)nF * FSTRIDE * 8; }
+  static constexpr size_t smem(int nF) { return stage_bytes(nF) + (size_t)nF * WY * PM * 8 + 16; }
+};
+
+template <int NX, int WY, int T>
+__global__ void __launch_bounds__(T, 1) x_pass_tma_kernel(const RunParams* __restrict__ runs, const Shape sh) {
+  using G = XTMA<NX, WY>;
+  constexpr int M = G::M, KX = G::KX, PM = G::PM;
+  using LM = Line<M>;
+  constexpr int NP = LM::N2 / 2 + 1;
+  extern __shared__ __align__(128) unsigned char xsm[];
+  const RunParams& rp = runs[blockIdx.y];
+  const int nF = rp.V + 1;
+  float2* stage = reinterpret_cast<float2*>(xsm);  // [nF][KX][WY], field stride FSTRIDE
+  float2* smem = reinterpret_cast<float2*>(xsm + G::stage_bytes(nF));  // lines [nF * WY][PM]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xsm + G::stage_bytes(nF) + (size_t)nF * WY * PM * 8);
+  const int ny_tiles = sh.Ny / WY;
+  const int ntiles = sh.Nz * ny_tiles;
+  const unsigned tile_bytes = (unsigned)(nF * KX * WY * 8);
+  const size_t plane = (size_t)sh.Nz * sh.Ny;
+  const size_t fstride = (size_t)sh.Kx * plane;
+  if (threadIdx.x == 0) mbar_init(bar, 1);
+  __syncthreads();
+  auto issue = [&](int t) {
+    const int zt = t / ny_tiles, yt = (t - zt * ny_tiles) * WY;
+    mbar_expect_tx(bar, tile_bytes);
+    for (int f = 0; f < nF; ++f) tma_load_4d(stage + (size_t)f * G::FSTRIDE, rp.tmap_sm, yt, zt, 0, f, bar);
+  };
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < ntiles) issue(tile);
+  unsigned parity = 0;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int z = tile / ny_tiles;
+    const int y0 = (tile - z * ny_tiles) * WY;
+    const size_t row_off = (size_t)z * sh.Ny + y0;
+    const bool ok = mbar_wait(bar, parity);
+    if (!__syncthreads_and(ok)) {  // the tile never arrived: flag the step and stop
+      if (threadIdx.x == 0) atomicOr(rp.err, 1u);
+      return;
+    }
+    parity ^= 1u;
+    // 1. inverse x transform from the staged half spectra (element kx of row yy at [kx][yy])
+    for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
+      const int l = it % (nF * WY), pr = it / (nF * WY);
+      const int f = l / WY, yy = l - f * WY;
+      x_inv_runs<M, true>(stage + (size_t)f * G::FSTRIDE + yy, WY, smem + l * PM, pr, sh.twN);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x);  // staging is free again
+    passA_rt<M, PM, T, true>(smem, nF * WY, sh.twM);
+    __syncthreads();
+    // 2. bulk terms
+    BulkAcc acc;
+    acc.init();
+    bulk_tile<NX, WY, T>(smem, rp, sh, z, y0, acc);
+    __syncthreads();
+    // 3. forward x transform -> D
+    passA_rt<M, PM, T, false>(smem, nF * WY, sh.twM);
+    __syncthreads();
+    const float scale = 1.0f / (float)NX;
+    for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
+      const int l = it % (nF * WY), pr = it / (nF * WY);
+      const int f = l / WY, yy = l - f * WY;
+      x_fwd_runs<M>(rp.D + f * fstride + row_off + yy, plane, smem + l * PM, pr, scale, sh.twN);
+    }
+    // 4. diagnostics of the tile (its block partials; ends with a barrier, so
+    //    the lines are free for the next tile afterwards)
+    store_block_diag<T>(acc, rp, sh, tile);
+    __syncthreads();
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -747,92 +931,116 @@ __device__ __forceinline__ void kpoint(const KPlane& P, const KRow& R, const flo
 // fixed order (the result does not depend on which CTA comes last), writes the
 // record into the ring, advances the step counter and resets the ticket.
 // The c planes may run as a second, concurrent launch: both draw from the
-// run's one ticket counter, sized for all nblk_yz CTAs.
+// run's one ticket counter, sized for all nblk_yz CTAs.  Sums are compensated
+// FP32 pairs up to the warp totals; the mass is then summed over the warps in
+// FP64 with compensation (KSum).
 // ---------------------------------------------------------------------------
 template <int T>
 __device__ __noinline__ void step_record(const RunParams& rp, const Shape& sh) {
   static_assert(T % 32 == 0 && T <= 1024, "whole warps");
-  __shared__ double sd[6][T / 32];  // f_eta, f_ch, mass (s, c), f_int, non-finite count
-  __shared__ float sf[4][T / 32];
+  constexpr int NW = T / 32;
+  __shared__ float sd[10][NW];  // hi, lo of f_eta, f_ch, mass, f_int (order parameters), f_int (c)
+  __shared__ float sf[4][NW];
+  __shared__ int si[NW];
   __threadfence();
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int nb = sh.nblk_x;
-  const double* __restrict__ px = rp.part_x;
-  double a_eta = 0, a_ch = 0, a_int = 0, a_bad = 0;
-  KSum a_mass;
+  const float* __restrict__ px = rp.part_x;
+  FF eta = ff(0.f), ch = ff(0.f), mass = ff(0.f), fphi = ff(0.f), fc = ff(0.f);
   float cmin = 1.f, cmax = 0.f, pmin = 1.f, ppmax = 0.f;  // reference start values (:1076-1079)
+  int bad = 0;
   for (int i = t; i < nb; i += T) {
-    a_eta += __ldcg(px + XD_FETA * nb + i);
-    a_ch += __ldcg(px + XD_FCH * nb + i);
-    a_mass.add(__ldcg(px + XD_MASS * nb + i));
-    cmin = fminf(cmin, (float)__ldcg(px + XD_CMIN * nb + i));
-    cmax = fmaxf(cmax, (float)__ldcg(px + XD_CMAX * nb + i));
-    pmin = fminf(pmin, (float)__ldcg(px + XD_PHIMIN * nb + i));
-    ppmax = fmaxf(ppmax, (float)__ldcg(px + XD_PHIPMAX * nb + i));
-    a_bad += __ldcg(px + XD_NONFINITE * nb + i);
+    eta.add(ff(__ldcg(px + XQ_FETA_H * nb + i), __ldcg(px + XQ_FETA_L * nb + i)));
+    ch.add(ff(__ldcg(px + XQ_FCH_H * nb + i), __ldcg(px + XQ_FCH_L * nb + i)));
+    mass.add(ff(__ldcg(px + XQ_MASS_H * nb + i), __ldcg(px + XQ_MASS_L * nb + i)));
+    cmin = fminf(cmin, __ldcg(px + XQ_CMIN * nb + i));
+    cmax = fmaxf(cmax, __ldcg(px + XQ_CMAX * nb + i));
+    pmin = fminf(pmin, __ldcg(px + XQ_PHIMIN * nb + i));
+    ppmax = fmaxf(ppmax, __ldcg(px + XQ_PHIPMAX * nb + i));
+    bad += (int)__ldcg(px + XQ_BAD * nb + i);
   }
-  for (int i = t; i < sh.nblk_yz; i += T) a_int += __ldcg(rp.part_yz + i);
-  a_eta = warp_sum(a_eta); a_ch = warp_sum(a_ch); a_int = warp_sum(a_int); a_bad = warp_sum(a_bad);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    KSum other;
-    other.s = __shfl_xor_sync(0xffffffffu, a_mass.s, o);
-    other.c = __shfl_xor_sync(0xffffffffu, a_mass.c, o);
-    a_mass.add(other);
+  // f_int partials: the last nblk_yz / nF slots belong to the c planes
+  const int nyz = sh.nblk_yz, cstart = nyz - nyz / (rp.V + 1);
+  for (int i = t; i < nyz; i += T) {
+    const FF v = ff(__ldcg(rp.part_yz + i), __ldcg(rp.part_yz + nyz + i));
+    if (i < cstart) fphi.add(v);
+    else fc.add(v);
   }
+  eta = warp_sum_ff(eta); ch = warp_sum_ff(ch); mass = warp_sum_ff(mass);
+  fphi = warp_sum_ff(fphi); fc = warp_sum_ff(fc);
   cmin = warp_min(cmin); cmax = warp_max(cmax); pmin = warp_min(pmin); ppmax = warp_max(ppmax);
+  bad = __reduce_add_sync(0xffffffffu, bad);
   if (lane == 0) {
-    sd[0][w] = a_eta; sd[1][w] = a_ch; sd[2][w] = a_mass.s; sd[3][w] = a_mass.c; sd[4][w] = a_int; sd[5][w] = a_bad;
+    sd[0][w] = eta.hi; sd[1][w] = eta.lo; sd[2][w] = ch.hi; sd[3][w] = ch.lo; sd[4][w] = mass.hi; sd[5][w] = mass.lo;
+    sd[6][w] = fphi.hi; sd[7][w] = fphi.lo; sd[8][w] = fc.hi; sd[9][w] = fc.lo;
     sf[0][w] = cmin; sf[1][w] = cmax; sf[2][w] = pmin; sf[3][w] = ppmax;
+    si[w] = bad;
   }
   __syncthreads();
-  if (t == 0) {
-    double e = 0, c = 0, fi = 0, bad = 0;
+  if (w == 0) {
+    const bool in = lane < NW;
+    const FF e = warp_sum_ff(in ? ff(sd[0][lane], sd[1][lane]) : ff(0.f));
+    const FF c = warp_sum_ff(in ? ff(sd[2][lane], sd[3][lane]) : ff(0.f));
+    const FF a = warp_sum_ff(in ? ff(sd[6][lane], sd[7][lane]) : ff(0.f));
+    const FF b = warp_sum_ff(in ? ff(sd[8][lane], sd[9][lane]) : ff(0.f));
+    // mass: the warps' compensated sums in FP64, combined with compensation
     KSum m;
-    float m0 = 1.f, m1 = 0.f, m2 = 1.f, m3 = 0.f;
-    for (int k = 0; k < T / 32; ++k) {
-      e += sd[0][k]; c += sd[1][k]; fi += sd[4][k]; bad += sd[5][k];
-      KSum o;
-      o.s = sd[2][k];
-      o.c = sd[3][k];
-      m.add(o);
-      m0 = fminf(m0, sf[0][k]); m1 = fmaxf(m1, sf[1][k]); m2 = fminf(m2, sf[2][k]); m3 = fmaxf(m3, sf[3][k]);
+    if (in) m.add(ff(sd[4][lane], sd[5][lane]).value());
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      KSum other;
+      other.s = __shfl_xor_sync(0xffffffffu, m.s, o);
+      other.c = __shfl_xor_sync(0xffffffffu, m.c, o);
+      m.add(other);
     }
-    const int step = *rp.counter;
-    double* d = rp.diag + (size_t)(step % rp.ring) * DR_COUNT;
-    d[DR_STEP] = step + 1;
-    d[DR_FINT] = fi;
-    d[DR_FETA] = e;
-    d[DR_FCH] = c;
-    d[DR_CMIN] = m0;
-    d[DR_CMAX] = m1;
-    d[DR_PHIMIN] = m2;
-    d[DR_PHIPMAX] = m3;
-    d[DR_MASS] = m.value();
-    d[DR_NONFINITE] = bad;
-    *rp.counter = step + 1;
-    *rp.ticket = 0u;  // the next step's yz pass starts after this launch ends
+    const float m0 = warp_min(in ? sf[0][lane] : 1.f), m1 = warp_max(in ? sf[1][lane] : 0.f);
+    const float m2 = warp_min(in ? sf[2][lane] : 1.f), m3 = warp_max(in ? sf[3][lane] : 0.f);
+    const int nbad = __reduce_add_sync(0xffffffffu, in ? si[lane] : 0);
+    if (lane == 0) {
+      const int step = *rp.counter;
+      double* d = rp.diag + (size_t)(step % rp.ring) * DR_COUNT;
+      const double n3 = (double)sh.Nx * sh.Ny * sh.Nz;
+      d[DR_STEP] = step + 1;
+      d[DR_FINT] = 0.5 * n3 * ((double)rp.kappa_phi * a.value() + (double)rp.kappa_c * b.value());
+      d[DR_FETA] = e.value();
+      d[DR_FCH] = c.value();
+      d[DR_CMIN] = m0;
+      d[DR_CMAX] = m1;
+      d[DR_PHIMIN] = m2;
+      d[DR_PHIPMAX] = m3;
+      d[DR_MASS] = m.value();
+      d[DR_NONFINITE] = nbad + (*rp.err ? 1e9 : 0.0);  // a failed TMA wait flags every later step
+      *rp.counter = step + 1;
+      *rp.ticket = 0u;  // the next step's yz pass starts after this launch ends
+    }
   }
 }
 
-// Store this CTA's f_int partial (coef times the block sum of the per-thread
-// FP32 sums) in slot `slot`, then draw the ticket; the last CTA forms the record.
+// Store this CTA's f_int partial -- w times the sum of the per-thread FP32
+// sums of |kf|^2 |u_hat|^2 (w = 2 for the kx planes that stand for their
+// conjugates, else 1) -- as a compensated pair in slot `slot`, then draw the
+// ticket; the last CTA forms the record.
 template <int T>
-__device__ __forceinline__ void yz_finish(const RunParams& rp, const Shape& sh, float fint, double coef, size_t slot) {
-  __shared__ double red[T / 32];
+__device__ __forceinline__ void yz_finish(const RunParams& rp, const Shape& sh, float fint, float w, size_t slot) {
+  constexpr int NW = T / 32;
+  __shared__ float red[2][NW];
   __shared__ int last;
-  const double v = (double)warp_sumf(fint);
+  const FF v = warp_sum_ff(ff(fint * w));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) red[wid] = v;
+  if (lane == 0) {
+    red[0][wid] = v.hi;
+    red[1][wid] = v.lo;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0;
-#pragma unroll
-    for (int q = 0; q < T / 32; ++q) s += red[q];
-    rp.part_yz[slot] = s * coef;
-    __threadfence();
-    const unsigned tk = atomicAdd(rp.ticket, 1u);
-    last = (tk + 1u == (unsigned)sh.nblk_yz);
+  if (wid == 0) {
+    const FF s = warp_sum_ff(lane < NW ? ff(red[0][lane], red[1][lane]) : ff(0.f));
+    if (lane == 0) {
+      rp.part_yz[slot] = s.hi;
+      rp.part_yz[sh.nblk_yz + slot] = s.lo;
+      __threadfence();
+      const unsigned tk = atomicAdd(rp.ticket, 1u);
+      last = (tk + 1u == (unsigned)sh.nblk_yz);
+    }
   }
   __syncthreads();
   if (last) step_record<T>(rp, sh);
@@ -1133,9 +1341,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
 
   if (MODE == YZ_MAIN) {
     // f_int partial (:609-678 by Parseval): 0.5 kappa N^3 w |kf|^2 |u_hat|^2
-    const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
-    const double n3 = (double)sh.Nx * NY * NZ;
-    yz_finish<T>(rp, sh, fint, wkx * 0.5 * kap * n3, (size_t)sh.plane0 * C + blockIdx.x);
+    yz_finish<T>(rp, sh, fint, wkx, (size_t)sh.plane0 * C + blockIdx.x);
   }
 }
 
@@ -1317,9 +1523,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   }
 
   if (MODE == YZ_MAIN) {
-    const double kap = is_c ? rp.kappa_c : rp.kappa_phi;
-    const double n3 = (double)sh.Nx * NY * NZ;
-    yz_finish<T>(rp, sh, fint, wkx * 0.5 * kap * n3, (size_t)p);
+    yz_finish<T>(rp, sh, fint, wkx, (size_t)p);
   }
 }
 

@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(kThreads) noalloc_cells_kernel(const float* __
   __shared__ double sd[4][kThreads / 32];
   __shared__ float sf[4][kThreads / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const double s0 = warp_sum_f32(feta), s1 = warp_sum_f32(fch), s2 = warp_sum_ff(mass);
+  const double s0 = warp_sum_f32(feta), s1 = warp_sum_f32(fch), s2 = warp_sum_ff(mass).value();
   const double s3 = (double)__reduce_add_sync(0xffffffffu, bad);
   const float m0 = warp_min(cmin), m1 = warp_max(cmax), m2 = warp_min(pmin), m3 = warp_max(ppmax);
   if (lane == 0) {

@@ -16,6 +16,7 @@ static int add(XKernels* out, int n) {
   k.wy = WY;
   k.threads = T;
   k.cl = 0;
+  k.tma = 0;
   k.bulk_smem = nullptr;
   return n + 1;
 }
@@ -23,6 +24,23 @@ static int add(XKernels* out, int n) {
 template <int NX, int WY>
 static size_t cl_smem(int nF) {
   return XCL<NX, WY>::smem(nF);
+}
+
+template <int NX, int WY>
+static size_t tma_smem(int nF) {
+  return XTMA<NX, WY>::smem(nF);
+}
+
+// bulk pass as the persistent TMA-staged kernel; the other modes use the plain kernel
+template <int NX, int WY, int T>
+static int addtma(XKernels* out, int n) {
+  if (n >= kMaxVariants) return n;
+  n = add<NX, WY, T>(out, n);
+  XKernels& k = out[n - 1];
+  k.bulk = x_pass_tma_kernel<NX, WY, T>;
+  k.tma = 1;
+  k.bulk_smem = tma_smem<NX, WY>;
+  return n;
 }
 
 // bulk pass split over two-CTA clusters; the other modes use the one-CTA kernel
@@ -44,6 +62,7 @@ int x_variants_a(int nx, XKernels* out, int n) {
     case 64:
       n = add<64, 8, 256>(out, n); n = add<64, 16, 256>(out, n); n = add<64, 4, 128>(out, n);
       n = addcl<64, 8, 256>(out, n);
+      n = addtma<64, 8, 512>(out, n);
       break;
     case 96:  // 512-thread CTAs keep 16 warps per SM when many fields leave room for one CTA only
       n = add<96, 8, 256>(out, n); n = add<96, 4, 256>(out, n); n = add<96, 16, 256>(out, n);
@@ -57,10 +76,12 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = add<128, 16, 256>(out, n);
       n = add<128, 4, 512>(out, n);
       n = addcl<128, 4, 256>(out, n); n = addcl<128, 8, 256>(out, n);
+      n = addtma<128, 8, 512>(out, n); n = addtma<128, 8, 256>(out, n);
       break;
     case 256:
       n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n);
       n = addcl<256, 4, 256>(out, n); n = addcl<256, 4, 512>(out, n);
+      n = addtma<256, 4, 512>(out, n);
       break;
     default: break;
   }

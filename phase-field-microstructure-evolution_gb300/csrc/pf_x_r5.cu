@@ -17,6 +17,7 @@ static int add(XKernels* out, int n) {
   k.wy = WY;
   k.threads = T;
   k.cl = 0;
+  k.tma = 0;
   k.bulk_smem = nullptr;
   return n + 1;
 }

@@ -9,8 +9,9 @@ workloads, so these tests use its own definitions):
 * the batched ensemble (16 runs of 64^3, P = 8, per-run L, kappa, g, c0 drawn
   from ran_2 seed 3): batched equals alone bit for bit, and every run matches
   the oracle;
-* the mass of c over 1000 steps: the compensated sum of the cell values stays
-  at N^3 Re c_hat(0), and that coefficient never changes.
+* the mass of c over 1000 steps: the k = 0 coefficient of c never changes,
+  and the compensated sum of the cell values stays at N^3 Re c_hat(0) to the
+  FP32 rounding of those values.
 
 Tolerance: max-abs and L2 error of every field relative to the reference's
 max-abs / L2 norm <= 1e-5 (FP32 path); diagnostics <= 1e-5 relative.  The
@@ -24,6 +25,13 @@ import bench
 from test_gpu_parity import TOL32, _check_diag, _check_fields, _l2, _rel, _run_lib
 
 pytestmark = pytest.mark.gpu
+
+# The mass is the compensated FP64 sum of the FP32 cell values the x pass
+# sees; those values carry the rounding of the inverse transforms, which for a
+# field close to a constant leans the same way in most cells (up to half an
+# FP32 ulp of c each: 3e-8 relative at c = 0.4).  Measured on the GB300:
+# 3e-8 to 7e-8 against the FP64 path and against N^3 Re c_hat(0).
+MASS_TOL = 2e-7
 
 
 def _workload(name):
@@ -44,7 +52,7 @@ def _check_records(gd, hd, tol):
         assert a["step"] == b["step"] and a["nonfinite"] == 0
         for k in ("f_int", "f_eta", "f_ch", "c_min", "c_max", "phi_min", "phi_P_max"):
             assert abs(a[k] - b[k]) <= tol * max(1.0, abs(b[k])), (a["step"], k, a[k], b[k])
-        assert abs(a["mass"] - b["mass"]) <= 1e-9 * abs(b["mass"]), (a["step"], a["mass"], b["mass"])
+        assert abs(a["mass"] - b["mass"]) <= MASS_TOL * abs(b["mass"]), (a["step"], a["mass"], b["mass"])
 
 
 def test_polycrystal_128_P16_vs_fp64_path_100_steps(pkg):
@@ -132,6 +140,6 @@ def test_mass_is_the_k0_coefficient_over_1000_steps(pkg, oracle, workload):
     exact = float(np.sum(con.astype(np.float32).astype(np.float64), dtype=np.float64))
     print(f"{workload}: |mass - N^3 Re c_hat(0)| <= {dev:.2e}, drift {drift:.2e}, "
           f"start vs sum of the FP32 start values {abs(gd[0]['mass'] - exact) / abs(exact):.2e}")
-    assert dev < 1e-8 and drift < 1e-8
+    assert dev < MASS_TOL and drift < MASS_TOL
     # the x pass sees c after one FP32 round trip through the transforms
-    assert abs(gd[0]["mass"] - exact) <= 1e-7 * abs(exact)
+    assert abs(gd[0]["mass"] - exact) <= 2e-8 * abs(exact)
