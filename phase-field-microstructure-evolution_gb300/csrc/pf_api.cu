@@ -141,6 +141,7 @@ static size_t x_smem(int nx, int nF, int wy) {
     case 80: pitch = Line<40>::PITCH; break;
     case 160: pitch = Line<80>::PITCH; break;
     case 200: pitch = Line<100>::PITCH; break;
+    case 102: pitch = Line<51>::PITCH; break;
     default: return 0;
   }
   return (size_t)nF * wy * pitch * sizeof(float2);
@@ -190,7 +191,7 @@ static int validate(const pf_config* c) {
   XKernels xv[kMaxVariants];
   YZKernels yk;
   const int nxv = get_x_variants(c->nx, xv);
-  if (nxv == 0) return fail(PF_EINVAL, "Nx=%d not supported (16, 32, 64, 80, 96, 128, 160, 200, 256)", c->nx);
+  if (nxv == 0) return fail(PF_EINVAL, "Nx=%d not supported (16, 32, 64, 80, 96, 102, 128, 160, 200, 256)", c->nx);
   if (!get_yz_kernels(c->ny, c->nz, &yk))
     return fail(PF_EINVAL, "(Ny, Nz)=(%d, %d) not supported by the fused FP32 path", c->ny, c->nz);
   if (c->var < 1 || c->var > kMaxVar) return fail(PF_EINVAL, "var=%d outside [1, %d]", c->var, kMaxVar);

@@ -14,7 +14,7 @@
 // takes that order back to natural order.  The spectral update in between is
 // pointwise, so no reordering pass is ever needed.
 //
-// Each DFT of size <= 20 lives in registers; in shared memory every run of N1
+// Each DFT of size <= 20 lives in registers (17 as a direct DFT); in shared memory every run of N1
 // consecutive elements is followed by one pad slot and the line pitch is odd,
 // which makes pass A, pass B and line-to-line transposes free of bank
 // conflicts for 8-byte complex elements.
@@ -56,6 +56,24 @@ PF_HD float2 cmul_pi(float2 a) { return make_float2(-a.y, a.x); }
 #define PF_C20_2 0.80901699437494742410f  // cos(pi/5)
 #define PF_C20_3 0.58778525229247312917f  // cos(3 pi/10)
 #define PF_C20_4 0.30901699437494742410f  // cos(2 pi/5)
+
+// cos and sin of 2 pi m / 17, m = 1..8 (the prime-17 DFT)
+#define PF_C17_1 0.932472229404355804573f
+#define PF_C17_2 0.739008917220659115925f
+#define PF_C17_3 0.445738355776538267396f
+#define PF_C17_4 0.0922683594633019952397f
+#define PF_C17_5 -0.273662990072082863539f
+#define PF_C17_6 -0.602634636379256389179f
+#define PF_C17_7 -0.850217135729614152134f
+#define PF_C17_8 -0.982973099683901778282f
+#define PF_S17_1 0.361241666187152948745f
+#define PF_S17_2 0.673695643646557211713f
+#define PF_S17_3 0.895163291355062322067f
+#define PF_S17_4 0.995734176295034521871f
+#define PF_S17_5 0.961825643172819070409f
+#define PF_S17_6 0.798017227280239503333f
+#define PF_S17_7 0.526432162877355800245f
+#define PF_S17_8 0.183749517816570331574f
 
 // W_R^j for R in {2,3,4,5,6,8,10,12,16,20} (forward sign), j in [0, R)
 template <int R>
@@ -167,6 +185,44 @@ struct Dft<5> {
   }
 };
 
+// Prime 17 as a direct DFT on the symmetric pairs t_j = x_j + x_{17-j},
+// d_j = x_j - x_{17-j} (j = 1..8): with theta = 2 pi jk / 17,
+//   X_k      = x0 + sum_j cos(theta) t_j - i sum_j sin(theta) d_j,
+//   X_{17-k} = x0 + sum_j cos(theta) t_j + i sum_j sin(theta) d_j   (k = 1..8).
+template <>
+struct Dft<17> {
+  PF_HD static void fwd(float2* v) {
+    const float C[9] = {1.f, PF_C17_1, PF_C17_2, PF_C17_3, PF_C17_4, PF_C17_5, PF_C17_6, PF_C17_7, PF_C17_8};
+    const float S[9] = {0.f, PF_S17_1, PF_S17_2, PF_S17_3, PF_S17_4, PF_S17_5, PF_S17_6, PF_S17_7, PF_S17_8};
+    float2 t[9], d[9], out[17];
+    const float2 x0 = v[0];
+    float2 sum = x0;
+#pragma unroll
+    for (int j = 1; j <= 8; ++j) {
+      t[j] = cadd(v[j], v[17 - j]);
+      d[j] = csub(v[j], v[17 - j]);
+      sum = cadd(sum, t[j]);
+    }
+#pragma unroll
+    for (int k = 1; k <= 8; ++k) {
+      float2 a = x0, b = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 1; j <= 8; ++j) {
+        const int m = (j * k) % 17;
+        const int mm = m <= 8 ? m : 17 - m;
+        const float sn = m <= 8 ? S[mm] : -S[mm];
+        a = make_float2(fmaf(C[mm], t[j].x, a.x), fmaf(C[mm], t[j].y, a.y));
+        b = make_float2(fmaf(sn, d[j].x, b.x), fmaf(sn, d[j].y, b.y));
+      }
+      out[k] = make_float2(a.x + b.y, a.y - b.x);
+      out[17 - k] = make_float2(a.x - b.y, a.y + b.x);
+    }
+    v[0] = sum;
+#pragma unroll
+    for (int k = 1; k < 17; ++k) v[k] = out[k];
+  }
+};
+
 // Composite R = R1*R2 in registers: x[n1 + R1*n2] -> X[k2 + R2*k1]
 template <int R1, int R2>
 struct DftComposite {
@@ -246,10 +302,12 @@ template <> struct Plan<24>  { static constexpr int N1 = 8,  N2 = 3; };
 template <> struct Plan<32>  { static constexpr int N1 = 8,  N2 = 4; };
 template <> struct Plan<40>  { static constexpr int N1 = 8,  N2 = 5; };
 template <> struct Plan<48>  { static constexpr int N1 = 8,  N2 = 6; };
+template <> struct Plan<51>  { static constexpr int N1 = 3,  N2 = 17; };
 template <> struct Plan<64>  { static constexpr int N1 = 8,  N2 = 8; };
 template <> struct Plan<80>  { static constexpr int N1 = 16, N2 = 5; };
 template <> struct Plan<96>  { static constexpr int N1 = 8,  N2 = 12; };
 template <> struct Plan<100> { static constexpr int N1 = 10, N2 = 10; };
+template <> struct Plan<102> { static constexpr int N1 = 6,  N2 = 17; };
 template <> struct Plan<128> { static constexpr int N1 = 16, N2 = 8; };
 template <> struct Plan<160> { static constexpr int N1 = 16, N2 = 10; };
 template <> struct Plan<192> { static constexpr int N1 = 16, N2 = 12; };

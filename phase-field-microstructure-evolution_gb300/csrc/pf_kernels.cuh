@@ -820,6 +820,8 @@ struct YZ {
   static constexpr int UA = LA * PY;
   static constexpr int UB = LB * PZ;
   static constexpr size_t SMEM = (size_t)(UA + UB) * sizeof(float2);
+  // in-place variant: the A and B layouts share one buffer
+  static constexpr size_t SMEM_INPL = (size_t)(UA > UB ? UA : UB) * sizeof(float2);
   static_assert(NZ % C == 0 && NY % C == 0, "cluster must divide the plane");
 };
 
@@ -1138,6 +1140,57 @@ __device__ __forceinline__ void exch_BA(float2* __restrict__ A, uint32_t B_base,
   }
 }
 
+// In-place exchanges: every thread first reads all the elements it will own
+// in the new layout from the cluster's old layouts (into registers), the
+// cluster waits until every CTA has read everything it needs, and then each
+// CTA overwrites its own buffer with the new layout.  One buffer per CTA
+// instead of two, so a quarter of a 256 x 256 plane (140 KB) fits one CTA.
+template <int NY, int NZ, int C, int T>
+__device__ __forceinline__ void exch_AB_inpl(float2* __restrict__ buf, uint32_t A_base, int r) {
+  using G = YZ<NY, NZ, C>;
+  constexpr int TOTAL = G::LB * NZ;
+  static_assert(T % G::LB == 0 && TOTAL % T == 0, "threads must cover whole rows");
+  constexpr int S = T / G::LB;
+  constexpr int ITER = TOTAL / T;
+  const int yl = threadIdx.x % G::LB;
+  const int z0 = threadIdx.x / G::LB;
+  const uint32_t src_off = (uint32_t)(Line<NY>::phys(r * G::LB + yl)) * 8u;
+  float2 v[ITER];
+#pragma unroll
+  for (int k = 0; k < ITER; ++k) {
+    const int z = z0 + k * S;
+    const int owner = z / G::LA, zl = z - owner * G::LA;
+    v[k] = ld_peer<C>(map_rank(A_base + (uint32_t)(zl * G::PY) * 8u + src_off, owner));
+  }
+  cluster_barrier<C>();  // every CTA holds its new layout in registers
+#pragma unroll
+  for (int k = 0; k < ITER; ++k) buf[yl * G::PZ + Line<NZ>::phys(z0 + k * S)] = v[k];
+  __syncthreads();
+}
+
+template <int NY, int NZ, int C, int T>
+__device__ __forceinline__ void exch_BA_inpl(float2* __restrict__ buf, uint32_t B_base, int r) {
+  using G = YZ<NY, NZ, C>;
+  constexpr int TOTAL = G::LA * NY;
+  static_assert(T % G::LA == 0 && TOTAL % T == 0, "threads must cover whole lines");
+  constexpr int S = T / G::LA;
+  constexpr int ITER = TOTAL / T;
+  const int zl = threadIdx.x % G::LA;
+  const int y0 = threadIdx.x / G::LA;
+  const uint32_t src_off = (uint32_t)(Line<NZ>::phys(r * G::LA + zl)) * 8u;
+  float2 v[ITER];
+#pragma unroll
+  for (int k = 0; k < ITER; ++k) {
+    const int y = y0 + k * S;
+    const int owner = y / G::LB, yl = y - owner * G::LB;
+    v[k] = ld_peer<C>(map_rank(B_base + (uint32_t)(yl * G::PZ) * 8u + src_off, owner));
+  }
+  cluster_barrier<C>();  // no CTA reads a peer's buffer after this point
+#pragma unroll
+  for (int k = 0; k < ITER; ++k) buf[zl * G::PY + Line<NY>::phys(y0 + k * S)] = v[k];
+  __syncthreads();
+}
+
 // pass A (forward or inverse) over NL lines of length L, pitch P, T threads
 template <int L, int NL, int P, int T, bool INV>
 __device__ __forceinline__ void passA(float2* buf, const float2* __restrict__ tw) {
@@ -1175,14 +1228,12 @@ __device__ __forceinline__ void passA(float2* buf, const float2* __restrict__ tw
 template <int L, int NL, int P, int T, bool INV>
 __device__ __forceinline__ void passB(float2* buf) {
   constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
-  static_assert(T % N2 == 0, "threads must be a multiple of N2");
-  const int k2 = threadIdx.x % N2;
   constexpr int ITEMS = NL * N2, ITER = (ITEMS + T - 1) / T;
 #pragma unroll
   for (int j = 0; j < ITER; ++j) {
     const int it = threadIdx.x + j * T;
     if (ITEMS % T != 0 && it >= ITEMS) break;
-    const int l = it / N2;
+    const int l = it / N2, k2 = it - l * N2;  // k2 is fixed per thread when N2 divides T
     float2* p = buf + l * P + k2 * (N1 + 1);
     float2 u[N1];
 #pragma unroll
@@ -1193,7 +1244,7 @@ __device__ __forceinline__ void passB(float2* buf) {
   }
 }
 
-template <int NY, int NZ, int C, int T, int MODE>
+template <int NY, int NZ, int C, int T, int MODE, bool INPL = false>
 __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = YZ<NY, NZ, C>;
   using LY = Line<NY>;
@@ -1204,7 +1255,7 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   __shared__ float4 qzt[NZ];  // kz factors of the k-space update
   stage_kz<NZ, T>(qzt, sh);   // read after the barriers of the forward passes
   float2* UA = smem;
-  float2* UB = smem + G::UA;
+  float2* UB = INPL ? smem : smem + G::UA;  // in place: both layouts in one buffer
   const RunParams& rp = runs[blockIdx.y];
   const int r = (C == 1) ? 0 : (int)(blockIdx.x % C);
   const int p = sh.plane0 + (int)(blockIdx.x / C);
@@ -1246,7 +1297,8 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   __syncthreads();
   passB<NY, G::LA, G::PY, T, false>(UA);
   cluster_barrier<C>();
-  exch_AB<NY, NZ, C, T>(UB, smem_addr(UA), r);
+  if constexpr (INPL) exch_AB_inpl<NY, NZ, C, T>(UB, smem_addr(UA), r);
+  else exch_AB<NY, NZ, C, T>(UB, smem_addr(UA), r);
   __syncthreads();
   passA<NZ, G::LB, G::PZ, T, false>(UB, sh.twZ);
   __syncthreads();
@@ -1303,8 +1355,12 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   __syncthreads();
   passA<NZ, G::LB, G::PZ, T, true>(UB, sh.twZ);
   cluster_barrier<C>();
-  exch_BA<NY, NZ, C, T>(UA, smem_addr(UB), r);
-  cluster_barrier<C>();  // no CTA reads a peer's buffers after this point
+  if constexpr (INPL) {
+    exch_BA_inpl<NY, NZ, C, T>(UA, smem_addr(UB), r);  // ends after the last peer read
+  } else {
+    exch_BA<NY, NZ, C, T>(UA, smem_addr(UB), r);
+    cluster_barrier<C>();  // no CTA reads a peer's buffers after this point
+  }
   passB<NY, G::LA, G::PY, T, true>(UA);
   __syncthreads();
 
@@ -1399,7 +1455,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   using LZ = Line<NZ>;
   constexpr int N1y = LY::N1, N2y = LY::N2, N1z = LZ::N1, N2z = LZ::N2;
   constexpr int PY = YZ1<NY, NZ, RAWP>::PY;
-  static_assert(T % N1y == 0 && T % N2y == 0, "thread count");
+  static_assert(T % 32 == 0, "whole warps");
   extern __shared__ float2 U[];
   __shared__ float4 qzt[NZ];  // kz factors of the k-space update
   stage_kz<NZ, T>(qzt, sh);   // read after the barriers of the forward passes
@@ -1416,16 +1472,19 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   // 1. forward y transform of all NZ rows, first pass straight from global
   {
     const float2* src = (MODE == YZ_MAIN) ? rp.D + poff : (MODE == YZ_C2 ? rp.J + kx * plane_elems : rp.Sm + poff);
-    const int n1 = threadIdx.x % N1y;
+    // twiddles: preloaded when every iteration of a thread has the same n1
+    constexpr bool FIXED = (T % N1y) == 0;
     float2 wt[N2y];
+    if constexpr (FIXED) {
 #pragma unroll
-    for (int k2 = 1; k2 < N2y; ++k2) wt[k2] = __ldg(sh.twY + n1 * k2);
+      for (int k2 = 1; k2 < N2y; ++k2) wt[k2] = __ldg(sh.twY + (threadIdx.x % N1y) * k2);
+    }
     constexpr int ITEMS = NZ * N1y, ITER = (ITEMS + T - 1) / T;
 #pragma unroll 4
     for (int j = 0; j < ITER; ++j) {
       const int it = threadIdx.x + j * T;
       if (ITEMS % T != 0 && it >= ITEMS) break;
-      const int z = it / N1y;
+      const int z = it / N1y, n1 = it - z * N1y;
       const float2* s = src + (size_t)z * NY + n1;
       float2 v[N2y];
 #pragma unroll
@@ -1434,7 +1493,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
       float2* d = U + z * PY + n1;
       d[0] = v[0];
 #pragma unroll
-      for (int k2 = 1; k2 < N2y; ++k2) d[k2 * (N1y + 1)] = cmul(v[k2], wt[k2]);
+      for (int k2 = 1; k2 < N2y; ++k2) d[k2 * (N1y + 1)] = cmul(v[k2], FIXED ? wt[k2] : __ldg(sh.twY + n1 * k2));
     }
   }
   __syncthreads();
@@ -1496,21 +1555,23 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   {
     const bool real_plane = (kx == 0) || (2 * kx == sh.Nx);  // the x-DFT of real data is real there
     float2* dst = var_c ? rp.J + kx * plane_elems : rp.Sm + poff;
-    const int n1 = threadIdx.x % N1y;
+    constexpr bool FIXED = (T % N1y) == 0;
     float2 wt[N2y];
+    if constexpr (FIXED) {
 #pragma unroll
-    for (int k2 = 1; k2 < N2y; ++k2) wt[k2] = __ldg(sh.twY + n1 * k2);
+      for (int k2 = 1; k2 < N2y; ++k2) wt[k2] = __ldg(sh.twY + (threadIdx.x % N1y) * k2);
+    }
     constexpr int ITEMS = NZ * N1y, ITER = (ITEMS + T - 1) / T;
 #pragma unroll 4
     for (int j = 0; j < ITER; ++j) {
       const int it = threadIdx.x + j * T;
       if (ITEMS % T != 0 && it >= ITEMS) break;
-      const int z = it / N1y;
+      const int z = it / N1y, n1 = it - z * N1y;
       const float2* sp = U + z * PY + n1;
       float2 v[N2y];
       v[0] = sp[0];
 #pragma unroll
-      for (int k2 = 1; k2 < N2y; ++k2) v[k2] = cmulc(sp[k2 * (N1y + 1)], wt[k2]);
+      for (int k2 = 1; k2 < N2y; ++k2) v[k2] = cmulc(sp[k2 * (N1y + 1)], FIXED ? wt[k2] : __ldg(sh.twY + n1 * k2));
       dft_inv<N2y>(v);
       float2* o = dst + (size_t)z * NY + n1;
 #pragma unroll

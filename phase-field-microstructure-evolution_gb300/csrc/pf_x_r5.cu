@@ -1,7 +1,8 @@
-// Instantiations of the x pass for the grids with a factor 5 (80, 160, 200:
-// the reference's weak-scaling grids, inputs/config.yaml:71-106): x lines of
-// M = Nx/2 = 40, 80, 100 complex points (plans 8 x 5, 16 x 5, 10 x 10).  The
-// first variant of a size is its default; the autotuner picks among them.
+// Instantiations of the x pass for the rest of the reference's weak-scaling
+// grids (inputs/config.yaml:71-106): 80, 160 and 200 (x lines of M = Nx/2 =
+// 40, 80, 100 complex points, plans 8 x 5, 16 x 5, 10 x 10) and 102 (M = 51,
+// plan 3 x 17).  The first variant of a size is its default; the autotuner
+// picks among them.
 #include "pf_internal.h"
 
 namespace pf {
@@ -49,6 +50,7 @@ int x_variants_r5(int nx, XKernels* out, int n) {
       n = add<200, 4, 256>(out, n); n = add<200, 8, 256>(out, n); n = add<200, 2, 256>(out, n);
       n = addcl<200, 4, 256>(out, n);
       break;
+    case 102: n = add<102, 6, 256>(out, n); n = add<102, 2, 256>(out, n); n = add<102, 3, 256>(out, n); break;
     default: break;
   }
   return n;

@@ -97,10 +97,10 @@ static void check_line(std::mt19937& g) {
 int main() {
   std::mt19937 g(12345);
   check_dft<2>(g); check_dft<3>(g); check_dft<4>(g); check_dft<5>(g); check_dft<6>(g); check_dft<8>(g);
-  check_dft<10>(g); check_dft<12>(g); check_dft<16>(g); check_dft<20>(g);
+  check_dft<10>(g); check_dft<12>(g); check_dft<16>(g); check_dft<17>(g); check_dft<20>(g);
   check_line<4>(g); check_line<8>(g); check_line<12>(g); check_line<16>(g); check_line<24>(g);
-  check_line<32>(g); check_line<40>(g); check_line<48>(g); check_line<64>(g); check_line<80>(g);
-  check_line<96>(g); check_line<100>(g); check_line<128>(g); check_line<160>(g); check_line<192>(g);
+  check_line<32>(g); check_line<40>(g); check_line<48>(g); check_line<51>(g); check_line<64>(g); check_line<80>(g);
+  check_line<96>(g); check_line<100>(g); check_line<102>(g); check_line<128>(g); check_line<160>(g); check_line<192>(g);
   check_line<200>(g); check_line<256>(g);
   return 0;
 }

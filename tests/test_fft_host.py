@@ -1,4 +1,4 @@
-"""The in-register DFTs (radix 2, 3, 4, 5 and their composites up to 20) and
+"""The in-register DFTs (radix 2, 3, 4, 5, their composites up to 20, and 17) and
 the four-step line plans of every supported line length, compiled for the
 host from the same header the kernels use and checked against a plain FP64
 DFT (tests/fft_host_check.cu).  No GPU needed; nvcc compiles the host code."""
@@ -29,13 +29,13 @@ def fft_report(tmp_path_factory):
     return rep
 
 
-@pytest.mark.parametrize("radix", [2, 3, 4, 5, 6, 8, 10, 12, 16, 20])
+@pytest.mark.parametrize("radix", [2, 3, 4, 5, 6, 8, 10, 12, 16, 17, 20])
 def test_register_dft_matches_fp64(fft_report, radix):
     fwd, inv = fft_report[("dft", radix)]
     assert fwd < TOL and inv < TOL, (radix, fwd, inv)
 
 
-@pytest.mark.parametrize("length", [4, 8, 12, 16, 24, 32, 40, 48, 64, 80, 96, 100, 128, 160, 192, 200, 256])
+@pytest.mark.parametrize("length", [4, 8, 12, 16, 24, 32, 40, 48, 51, 64, 80, 96, 100, 102, 128, 160, 192, 200, 256])
 def test_line_plan_matches_fp64(fft_report, length):
     (err,) = fft_report[("line", length)]
     assert err < TOL, (length, err)
