@@ -238,7 +238,7 @@ struct pf_batch {
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t side = nullptr;        // second branch of the captured step (concentration chain)
   cudaStream_t copy = nullptr;        // record copies of completed steps (never waits for later steps)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_c = nullptr;
   int prio_hi = 0;                    // greatest stream priority of the device
   int nsm = 0;                        // multiprocessors of the device (persistent TMA x pass)
   std::vector<double> hdiag;
@@ -328,8 +328,16 @@ static int launch_x_bulk(pf_batch* b, cudaStream_t s) {
 // mobility, the concentration field's chain -- its yz planes, the xj pass and
 // the yz C2 pass, which the order-parameter planes do not need -- runs on a
 // second branch at high priority beside the order-parameter planes, so that
-// its small launches fill SMs as the big launch drains.  The step's record is
-// formed by whichever yz-pass CTA of a run finishes last (either branch).
+// its small launches fill SMs as the big launch drains; the record of the
+// step follows the order-parameter planes once the c planes' f_int partials
+// are in, beside the rest of the concentration chain.
+static constexpr int kRecordThreads = 1024;
+static int launch_record(pf_batch* b, cudaStream_t s) {
+  record_kernel<kRecordThreads><<<b->nruns, kRecordThreads, 0, s>>>(b->drp, b->tab.sh);
+  PF_CUDA(cudaGetLastError());
+  return PF_OK;
+}
+
 static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
   const int R = b->nruns;
   {
@@ -343,12 +351,16 @@ static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
     PF_CUDA(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     int rc = launch_yz(b, b->yk.main, b->Kx, b->drp, R, b->side, pc, b->prio_hi);
     if (rc) return rc;
+    PF_CUDA(cudaEventRecord(b->ev_c, b->side));
     rc = launch_xj(b, b->side, b->prio_hi);
     if (rc) return rc;
     rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, b->side, 0, b->prio_hi);
     if (rc) return rc;
     PF_CUDA(cudaEventRecord(b->ev_join, b->side));
     rc = launch_yz(b, b->yk.main, pc, b->drp, R, s);
+    if (rc) return rc;
+    PF_CUDA(cudaStreamWaitEvent(s, b->ev_c, 0));
+    rc = launch_record(b, s);
     if (rc) return rc;
     PF_CUDA(cudaStreamWaitEvent(s, b->ev_join, 0));
     return PF_OK;
@@ -361,7 +373,7 @@ static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
     rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, s);
     if (rc) return rc;
   }
-  return PF_OK;
+  return launch_record(b, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -612,7 +624,7 @@ static int tune_batch(pf_batch* b) {
         PF_CUDA(cudaMemsetAsync(r.Sk, 0, fbytes, b->stream));
         PF_CUDA(cudaMemsetAsync(r.Sm, 0, fbytes, b->stream));
         PF_CUDA(cudaMemsetAsync(r.D, 0, fbytes, b->stream));
-        PF_CUDA(cudaMemsetAsync(r.counter, 0, 256, b->stream));  // step counter, ticket, error word
+        PF_CUDA(cudaMemsetAsync(r.counter, 0, 256, b->stream));  // step counter, error word
       }
       PF_CUDA(cudaStreamSynchronize(b->stream));
       g_tune_cache[key] = std::make_tuple(bx, by, bj);
@@ -639,6 +651,7 @@ static void destroy_batch(pf_batch* b) {
   if (b->copy) cudaStreamDestroy(b->copy);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->ev_c) cudaEventDestroy(b->ev_c);
   cudaFree(b->drp);
   cudaFree(b->mem);
   cudaFree(b->fin);
@@ -693,7 +706,7 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   const size_t szPx = align((size_t)XD_COUNT * b->Nz * b->Ny * sizeof(double));
   const size_t szPyz = align((size_t)16 * b->nF * b->Kx * sizeof(double));
   const size_t szDiag = align((size_t)b->ring * DR_COUNT * sizeof(double));
-  const size_t szCnt = 256;   // step counter, ticket, error word (one 64-byte line each)
+  const size_t szCnt = 256;   // step counter and error word (one 64-byte line each)
   const size_t szTmap = 256;  // TMA tensor map of Sm (128 bytes, 64-byte aligned)
   const size_t per_run = 3 * szS + szMob + szJ + szPx + szPyz + szDiag + szCnt + szTmap;
   e = cudaMalloc(&b->mem, per_run * nruns);
@@ -724,7 +737,6 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
     r.part_yz = (float*)p; p += szPyz;
     r.diag = (double*)p; p += szDiag;
     r.counter = (int*)p;
-    r.ticket = (unsigned*)(p + 64);  // own 64-byte line in the 256-byte counter block
     r.err = (unsigned*)(p + 128);
     p += szCnt;
     r.tmap_sm = p;
@@ -755,6 +767,7 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   cudaDeviceGetStreamPriorityRange(&prio_lo, &b->prio_hi);
   e = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, b->prio_hi);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_c, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream/events: %s", cudaGetErrorString(e)));
@@ -790,7 +803,7 @@ static int batch_set_fields(pf_batch* b, int run, const double* phi, const doubl
   b->xk.imp<<<gx, b->xk.threads, b->smem_x, b->stream>>>(b->drp + run, b->tab.sh);
   int rc = launch_yz(b, b->yk.imp, b->nF * b->Kx, b->drp + run, 1, b->stream);
   if (rc) return rc;
-  PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, 256, b->stream));  // step counter, ticket, error word
+  PF_CUDA(cudaMemsetAsync(b->hrp[run].counter, 0, 256, b->stream));  // step counter, error word
   PF_CUDA(cudaGetLastError());
   PF_CUDA(cudaStreamSynchronize(b->stream));
   b->steps_done[run] = 0;

@@ -63,7 +63,6 @@ struct RunParams {
   float* part_yz;  // [2][nblk_yz]: hi and lo of each yz CTA's weighted f_int sum
   double* diag;    // [ring][DR_COUNT]
   int* counter;    // step counter (device)
-  unsigned* ticket;  // CTAs of the step's yz pass that have finished (reset by the last one)
   unsigned* err;     // bit 0: a TMA tile of the x pass never arrived (the step's record is flagged)
   const void* tmap_sm;  // TMA tensor map over Sm [nF][Kx][Nz][Ny] (x pass TMA variant), global memory
   float* fin;      // [nF][Nz][Ny][Nx] real fields for import/export
@@ -387,20 +386,17 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
   const float sg1 = rp.sigma1, sg2 = rp.sigma2;
   float2* base = smem + yy * PM + slot;
   constexpr int FS = WY * PM;  // stride between fields
-  // pass 1: S2 = sum phi^2, Smat = sum_{i<V-1} phi^2, S4, N4, f_eta pair sum
-  float pre0 = 0.f, pre1 = 0.f, n40 = 0.f, n41 = 0.f, pr0 = 0.f, pr1 = 0.f, ma0 = 0.f, ma1 = 0.f;
+  // pass 1: S2 = sum phi^2, Smat = sum_{i<V-1} phi^2, S4, N4, f_eta pair
+  // sum, both cells of the slot at once in packed FP32 pairs
+  float2 pre = make_float2(0.f, 0.f), n4v = make_float2(0.f, 0.f), prs = make_float2(0.f, 0.f);
   for (int f = 0; f < V - 1; ++f) {
     const float2 p = base[f * FS];
-    const float a0 = p.x * p.x, a1 = p.y * p.y;
-    pr0 = fmaf(a0, pre0, pr0);
-    pr1 = fmaf(a1, pre1, pr1);
-    pre0 += a0;
-    pre1 += a1;
-    n40 = fmaf(a0, a0, n40);
-    n41 = fmaf(a1, a1, n41);
-    ma0 = fmaxf(ma0, fabsf(p.x));
-    ma1 = fmaxf(ma1, fabsf(p.y));
+    const float2 a = __fmul2_rn(p, p);
+    prs = __ffma2_rn(a, pre, prs);
+    pre = __fadd2_rn(pre, a);
+    n4v = __ffma2_rn(a, a, n4v);
   }
+  const float pre0 = pre.x, pre1 = pre.y, n40 = n4v.x, n41 = n4v.y, pr0 = prs.x, pr1 = prs.y;
   const float2 pP = base[(V - 1) * FS];
   const float2 cc = base[V * FS];
   float2 out_df[2];
@@ -414,7 +410,6 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
     const float pre = q ? pre1 : pre0;
     const float n4 = q ? n41 : n40;
     const float pairs = q ? pr1 : pr0;
-    const float mabs = fmaxf(q ? ma1 : ma0, fabsf(pp));
     const float pp2 = pp * pp;
     const float S2 = pre + pp2;
     const float S4 = n4 + pp2 * pp2;
@@ -422,6 +417,14 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
     // (|phi| < ~1e-8) FP32 would lose them: rescale phi by 1/max|phi|.  All-zero
     // cells give 0/0 in the reference; here h = 0 and term4 = 0.
     float invS4, n4n, sc, im = 1.f;
+    float mabs = 0.f;
+    if (S4 < 1e-30f) {  // rare: max |phi| of the cell for the rescaled branch
+      mabs = fabsf(pp);
+      for (int f = 0; f < V - 1; ++f) {
+        const float2 p = base[f * FS];
+        mabs = fmaxf(mabs, fabsf(q ? p.y : p.x));
+      }
+    }
     if (S4 >= 1e-30f) {
       invS4 = 1.f / S4;
       n4n = n4 * invS4;
@@ -473,16 +476,38 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
   dfdc = make_float2(out_df[0].x, out_df[1].x);
   mob = make_float2(out_df[0].y, out_df[1].y);
   // pass 2: dF/dphi_i = phi^3 - phi + 2 phi Gamma_i + term4_i   (:782-857)
+  // with Gamma_i = sigma1 (Smat - phi_i^2) + sigma2 phiP^2 and term4_i =
+  // t4a q_i^3, q_i = phi_i / max|phi| (the rescaled branch) or phi_i.
   float dsum = dfdc.x + dfdc.y;
-  for (int f = 0; f < V - 1; ++f) {
-    float2 p = base[f * FS];
-    const float g0 = fmaf(sg1, Smat[0] - p.x * p.x, gP[0]);
-    const float g1 = fmaf(sg1, Smat[1] - p.y * p.y, gP[1]);
-    const float q0 = p.x * invm[0], q1 = p.y * invm[1];
-    const float d0 = fmaf(p.x, p.x * p.x, -p.x) + 2.f * p.x * g0 + t4a[0] * (q0 * q0 * q0);
-    const float d1 = fmaf(p.y, p.y * p.y, -p.y) + 2.f * p.y * g1 + t4a[1] * (q1 * q1 * q1);
-    dsum += d0 + d1;
-    base[f * FS] = make_float2(d0, d1);
+  if (invm[0] == 1.f && invm[1] == 1.f) {
+    // packed over the slot's two cells:
+    //   dF = phi (2 sigma1 (Smat - phi^2) + phi^2 (1 + t4a) + 2 gP - 1)
+    const float2 two_s1 = make_float2(2.f * sg1, 2.f * sg1), m1 = make_float2(-1.f, -1.f);
+    const float2 opt4 = make_float2(1.f + t4a[0], 1.f + t4a[1]);
+    const float2 cterm = make_float2(fmaf(2.f, gP[0], -1.f), fmaf(2.f, gP[1], -1.f));
+    const float2 sm = make_float2(Smat[0], Smat[1]);
+    float2 ds = make_float2(0.f, 0.f);
+    for (int f = 0; f < V - 1; ++f) {
+      const float2 p = base[f * FS];
+      const float2 p2 = __fmul2_rn(p, p);
+      const float2 sd = __ffma2_rn(p2, m1, sm);                              // Smat - phi^2
+      const float2 h = __ffma2_rn(sd, two_s1, __ffma2_rn(p2, opt4, cterm));
+      const float2 d = __fmul2_rn(p, h);
+      ds = __fadd2_rn(ds, d);
+      base[f * FS] = d;
+    }
+    dsum += ds.x + ds.y;
+  } else {
+    for (int f = 0; f < V - 1; ++f) {
+      float2 p = base[f * FS];
+      const float g0 = fmaf(sg1, Smat[0] - p.x * p.x, gP[0]);
+      const float g1 = fmaf(sg1, Smat[1] - p.y * p.y, gP[1]);
+      const float q0 = p.x * invm[0], q1 = p.y * invm[1];
+      const float d0 = fmaf(p.x, p.x * p.x, -p.x) + 2.f * p.x * g0 + t4a[0] * (q0 * q0 * q0);
+      const float d1 = fmaf(p.y, p.y * p.y, -p.y) + 2.f * p.y * g1 + t4a[1] * (q1 * q1 * q1);
+      dsum += d0 + d1;
+      base[f * FS] = make_float2(d0, d1);
+    }
   }
   {
     const float g0 = sg2 * Smat[0], g1 = sg2 * Smat[1];
@@ -545,12 +570,24 @@ __device__ __forceinline__ void store_block_diag(const BulkAcc& acc, const RunPa
 // physical slots of the padded lines and the pad slots stay idle, so that the
 // 16 slots of a half warp always fall in distinct bank pairs (a walk over the
 // logical cells would span 17 slots and put its first and last in one pair).
-template <int NX, int WY, int T>
+template <int NX, int WY, int T, bool PHYS = true>
 __device__ __forceinline__ void bulk_tile(float2* smem, const RunParams& rp, const Shape& sh, int z, int y0,
                                           BulkAcc& acc) {
   constexpr int M = NX / 2;
   using LM = Line<M>;
   constexpr int PM = LM::PITCH, N1 = LM::N1;
+  if constexpr (!PHYS) {  // walk over the logical cells (a half warp spans N1 + 1 slots per N1 cells)
+    for (int it = threadIdx.x; it < WY * M; it += T) {
+      const int m = it % M, yy = it / M;
+      const int slot = LM::phys(m);
+      float2 dfdc, mob;
+      bulk_slot<PM, WY>(smem, yy, slot, rp, dfdc, mob, acc);
+      smem[(rp.V * WY + yy) * PM + slot] = dfdc;
+      if (rp.mobility != MOB_CONST)
+        *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = mob;
+    }
+    return;
+  }
   for (int it = threadIdx.x; it < WY * PM; it += T) {
     const int yy = it / PM, ps = it - yy * PM;
     const int q = ps / (N1 + 1), r = ps - q * (N1 + 1);
@@ -617,7 +654,7 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, int c0,
 // ---------------------------------------------------------------------------
 enum XMode { MODE_BULK = 0, MODE_XJ = 1, MODE_IMPORT = 2, MODE_EXPORT = 3 };
 
-template <int NX, int WY, int T, int MODE>
+template <int NX, int WY, int T, int MODE, bool PHYS = true>
 __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   constexpr int M = NX / 2;
   using LM = Line<M>;
@@ -671,7 +708,7 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
 
   if (MODE == MODE_BULK) {
     // 2. bulk terms, two cells per slot
-    bulk_tile<NX, WY, T>(smem, rp, sh, z, y0, acc);
+    bulk_tile<NX, WY, T, PHYS>(smem, rp, sh, z, y0, acc);
     __syncthreads();
   } else if (MODE == MODE_XJ) {
     for (int it = threadIdx.x; it < WY * M; it += T) {
@@ -926,25 +963,23 @@ __device__ __forceinline__ void kpoint(const KPlane& P, const KRow& R, const flo
 }
 
 // ---------------------------------------------------------------------------
-// The step's record (src/var_diff.f90:1058-1118) is formed at the end of the
-// yz pass, with no separate launch: every CTA of a run's YZ_MAIN launches
-// stores its f_int partial and draws a ticket; the CTA that draws the last
-// one reduces the x-pass partials and all f_int partials of the run in a
-// fixed order (the result does not depend on which CTA comes last), writes the
-// record into the ring, advances the step counter and resets the ticket.
-// The c planes may run as a second, concurrent launch: both draw from the
-// run's one ticket counter, sized for all nblk_yz CTAs.  Sums are compensated
-// FP32 pairs up to the warp totals; the mass is then summed over the warps in
-// FP64 with compensation (KSum).
+// The step's record (src/var_diff.f90:1058-1118): one CTA per run reduces the
+// x-pass partials and the yz pass's f_int partials in a fixed order (the same
+// bits whichever other runs share the launch), writes the record into the
+// ring and advances the step counter.  Sums are compensated FP32 pairs up to
+// the warp totals; the mass is then summed over the warps in FP64 with
+// compensation (KSum).  A separate launch, not the last CTA of the yz pass:
+// the fence a CTA needs before announcing its partial holds that CTA (and the
+// SM's next one) until all of its stores have drained.
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ __noinline__ void step_record(const RunParams& rp, const Shape& sh) {
+__global__ void __launch_bounds__(T) record_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   static_assert(T % 32 == 0 && T <= 1024, "whole warps");
   constexpr int NW = T / 32;
   __shared__ float sd[10][NW];  // hi, lo of f_eta, f_ch, mass, f_int (order parameters), f_int (c)
   __shared__ float sf[4][NW];
   __shared__ int si[NW];
-  __threadfence();
+  const RunParams& rp = runs[blockIdx.x];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int nb = sh.nblk_x;
   const float* __restrict__ px = rp.part_x;
@@ -1013,20 +1048,17 @@ __device__ __noinline__ void step_record(const RunParams& rp, const Shape& sh) {
       d[DR_MASS] = m.value();
       d[DR_NONFINITE] = nbad + (*rp.err ? 1e9 : 0.0);  // a failed TMA wait flags every later step
       *rp.counter = step + 1;
-      *rp.ticket = 0u;  // the next step's yz pass starts after this launch ends
     }
   }
 }
 
 // Store this CTA's f_int partial -- w times the sum of the per-thread FP32
 // sums of |kf|^2 |u_hat|^2 (w = 2 for the kx planes that stand for their
-// conjugates, else 1) -- as a compensated pair in slot `slot`, then draw the
-// ticket; the last CTA forms the record.
+// conjugates, else 1) -- as a compensated pair in slot `slot`.
 template <int T>
 __device__ __forceinline__ void yz_finish(const RunParams& rp, const Shape& sh, float fint, float w, size_t slot) {
   constexpr int NW = T / 32;
   __shared__ float red[2][NW];
-  __shared__ int last;
   const FF v = warp_sum_ff(ff(fint * w));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) {
@@ -1039,13 +1071,8 @@ __device__ __forceinline__ void yz_finish(const RunParams& rp, const Shape& sh, 
     if (lane == 0) {
       rp.part_yz[slot] = s.hi;
       rp.part_yz[sh.nblk_yz + slot] = s.lo;
-      __threadfence();
-      const unsigned tk = atomicAdd(rp.ticket, 1u);
-      last = (tk + 1u == (unsigned)sh.nblk_yz);
     }
   }
-  __syncthreads();
-  if (last) step_record<T>(rp, sh);
 }
 
 template <int C>

@@ -43,6 +43,15 @@ static int addtma(XKernels* out, int n) {
   return n;
 }
 
+// bulk pass walking the logical cells (for comparison with the physical-slot walk)
+template <int NX, int WY, int T>
+static int addlog(XKernels* out, int n) {
+  if (n >= kMaxVariants) return n;
+  n = add<NX, WY, T>(out, n);
+  out[n - 1].bulk = x_pass_kernel<NX, WY, T, MODE_BULK, false>;
+  return n;
+}
+
 // bulk pass split over two-CTA clusters; the other modes use the one-CTA kernel
 template <int NX, int WY, int T>
 static int addcl(XKernels* out, int n) {
@@ -77,11 +86,12 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = add<128, 4, 512>(out, n);
       n = addcl<128, 4, 256>(out, n); n = addcl<128, 8, 256>(out, n);
       n = addtma<128, 8, 512>(out, n); n = addtma<128, 8, 256>(out, n);
+      n = addlog<128, 8, 256>(out, n);
       break;
     case 256:
       n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n);
       n = addcl<256, 4, 256>(out, n); n = addcl<256, 4, 512>(out, n);
-      n = addtma<256, 4, 512>(out, n);
+      n = addtma<256, 4, 512>(out, n); n = addtma<256, 2, 512>(out, n);
       break;
     default: break;
   }
