@@ -241,6 +241,7 @@ struct pf_batch {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_c = nullptr;
   int prio_hi = 0;                    // greatest stream priority of the device
   int nsm = 0;                        // multiprocessors of the device (persistent TMA x pass)
+  int tma_occ = 1;                    // resident CTAs per SM of the chosen TMA x pass
   std::vector<double> hdiag;
   std::vector<int> steps_done;
   std::string variant;  // chosen kernel variants, for reports
@@ -297,8 +298,8 @@ static int launch_xj(pf_batch* b, cudaStream_t s, int prio = 0) {
 static int launch_x_bulk(pf_batch* b, cudaStream_t s) {
   const int R = b->nruns;
   const unsigned nblk = (unsigned)(b->Nz * (b->Ny / b->xk.wy));
-  if (b->xk.tma) {  // persistent: about one CTA per SM over all runs
-    const unsigned g = (unsigned)std::max(1, std::min((int)nblk, b->nsm / R));
+  if (b->xk.tma) {  // persistent: as many CTAs as are resident at once, over all runs
+    const unsigned g = (unsigned)std::max(1, std::min((int)nblk, b->nsm * b->tma_occ / R));
     b->xk.bulk<<<dim3(g, R), b->xk.threads, b->smem_bulk, s>>>(b->drp, b->tab.sh);
     PF_CUDA(cudaGetLastError());
     return PF_OK;
@@ -517,7 +518,16 @@ static void apply_variants(pf_batch* b, const XKernels& xk, const YZKernels& yk)
   b->yk = yk;
   b->smem_x = x_smem(b->Nx, b->nF, xk.wy);
   b->smem_bulk = (xk.cl || xk.tma) ? xk.bulk_smem(b->nF) : b->smem_x;
-  if (xk.tma) write_tensor_maps(b, xk.wy);  // encodable: checked by x_ok
+  if (xk.tma) {
+    write_tensor_maps(b, xk.wy);  // encodable: checked by x_ok
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)xk.bulk, xk.threads, b->smem_bulk) !=
+            cudaSuccess || occ < 1) {
+      cudaGetLastError();
+      occ = 1;
+    }
+    b->tma_occ = std::min(occ, xk.tma);
+  }
   b->tab.sh.nblk_x = b->Nz * (b->Ny / xk.wy);
   b->tab.sh.nblk_yz = yk.cluster * b->nF * b->Kx;
   apply_xj(b, xk);

@@ -16,7 +16,7 @@ struct XKernels {
   int wy;       // y rows per CTA
   int threads;  // threads per CTA
   int cl = 0;   // 2: the bulk kernel runs as clusters of two CTAs sharing the fields (x_pass_cl_kernel)
-  int tma = 0;  // 1: the bulk kernel is the persistent TMA-staged x_pass_tma_kernel (one CTA per SM)
+  int tma = 0;  // > 0: the bulk kernel is the persistent TMA-staged x_pass_tma_kernel, at most this many CTAs per SM
   size_t (*bulk_smem)(int nF) = nullptr;  // its dynamic shared memory (cluster and TMA variants)
 };
 

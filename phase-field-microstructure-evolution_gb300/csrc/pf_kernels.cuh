@@ -744,8 +744,9 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
 // ---------------------------------------------------------------------------
 // x pass (bulk mode) with TMA-staged loads, persistent over tiles.
 //
-// Each CTA owns one SM and walks the tiles (WY rows at one z, all fields)
-// tile = blockIdx.x, blockIdx.x + gridDim.x, ...  The mixed-space half spectra
+// MINB CTAs per SM (the grid holds as many as are resident at once) walk the
+// tiles (WY rows at one z, all fields) tile = blockIdx.x, blockIdx.x +
+// gridDim.x, ...  The mixed-space half spectra
 // of a tile arrive by TMA -- one box {WY rows, 1 z, Kx, 1 field} per field of
 // the run's tensor map over Sm [nF][Kx][Nz][Ny] -- into a staging buffer
 // [field][kx][row]; as soon as the inverse x transform has consumed them,
@@ -765,8 +766,8 @@ struct XTMA {
   static constexpr size_t smem(int nF) { return stage_bytes(nF) + (size_t)nF * WY * PM * 8 + 16; }
 };
 
-template <int NX, int WY, int T>
-__global__ void __launch_bounds__(T, 1) x_pass_tma_kernel(const RunParams* __restrict__ runs, const Shape sh) {
+template <int NX, int WY, int T, int MINB = 1>
+__global__ void __launch_bounds__(T, MINB) x_pass_tma_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = XTMA<NX, WY>;
   constexpr int M = G::M, KX = G::KX, PM = G::PM;
   using LM = Line<M>;

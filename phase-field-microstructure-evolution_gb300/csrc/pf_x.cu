@@ -31,14 +31,15 @@ static size_t tma_smem(int nF) {
   return XTMA<NX, WY>::smem(nF);
 }
 
-// bulk pass as the persistent TMA-staged kernel; the other modes use the plain kernel
-template <int NX, int WY, int T>
+// bulk pass as the persistent TMA-staged kernel, at most MINB CTAs per SM;
+// the other modes use the plain kernel
+template <int NX, int WY, int T, int MINB = 1>
 static int addtma(XKernels* out, int n) {
   if (n >= kMaxVariants) return n;
   n = add<NX, WY, T>(out, n);
   XKernels& k = out[n - 1];
-  k.bulk = x_pass_tma_kernel<NX, WY, T>;
-  k.tma = 1;
+  k.bulk = x_pass_tma_kernel<NX, WY, T, MINB>;
+  k.tma = MINB;
   k.bulk_smem = tma_smem<NX, WY>;
   return n;
 }
@@ -87,6 +88,7 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = addcl<128, 4, 256>(out, n); n = addcl<128, 8, 256>(out, n);
       n = addtma<128, 8, 512>(out, n); n = addtma<128, 8, 256>(out, n);
       n = addlog<128, 8, 256>(out, n);
+      n = addtma<128, 4, 256, 3>(out, n); n = addtma<128, 4, 384, 2>(out, n);
       break;
     case 256:
       n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n);
