@@ -82,7 +82,8 @@ typedef struct pf_run pf_run;
 
 /* Create a run on cfg->device: validates the sizes, allocates the resident
  * state and builds the FP64 wavenumber/twiddle tables.  Supported grids on
- * the fused FP32 path: Nx, Ny, Nz in {16, 32, 64, 96, 128, 256} (every
+ * the fused FP32 path: Nx, Ny, Nz in {16, 32, 64, 80, 96, 102, 128, 160,
+ * 200, 256} (the reference's weak-scaling grids included; every
  * (Ny, Nz) pair with Ny == Nz plus the non-cubic pairs listed by
  * pf_supported_shape), 1 <= var <= 255 as long as var+1 field rows of the x
  * pass fit in shared memory (var <= 131 at Nx = 96, 98 at 128, 105 at 256).
