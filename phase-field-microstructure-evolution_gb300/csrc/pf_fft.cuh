@@ -27,8 +27,21 @@ namespace pf {
 // that tests can check them against a reference DFT on the CPU.
 #define PF_HD __host__ __device__ __forceinline__
 
-PF_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-PF_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// complex add and subtract: one packed FP32-pair instruction each on the device
+PF_HD float2 cadd(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+PF_HD float2 csub(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+#else
+  return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
 PF_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 PF_HD float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 // a * b
@@ -118,6 +131,8 @@ PF_HD float2 wconst<3>(int j) { return wconst<12>(4 * j); }
 // ---------------------------------------------------------------------------
 template <int R>
 struct Dft;
+template <int R>
+PF_HD void dft_inv(float2* v);
 
 template <>
 struct Dft<1> {
@@ -149,16 +164,21 @@ struct Dft<3> {
 
 template <>
 struct Dft<4> {
-  PF_HD static void fwd(float2* v) {
-    float2 t0 = cadd(v[0], v[2]);
-    float2 t1 = csub(v[0], v[2]);
-    float2 t2 = cadd(v[1], v[3]);
-    float2 t3 = cmul_mi(csub(v[1], v[3]));
+  // INV: +i instead of -i in the odd outputs; (v1 - v3) times -i (or +i) is
+  // formed directly in swapped order, so the butterflies stay packed pairs.
+  template <bool INV>
+  PF_HD static void run(float2* v) {
+    const float2 t0 = cadd(v[0], v[2]);
+    const float2 t1 = csub(v[0], v[2]);
+    const float2 t2 = cadd(v[1], v[3]);
+    const float2 t3 = INV ? make_float2(v[3].y - v[1].y, v[1].x - v[3].x)   // +i (v1 - v3)
+                          : make_float2(v[1].y - v[3].y, v[3].x - v[1].x);  // -i (v1 - v3)
     v[0] = cadd(t0, t2);
     v[2] = csub(t0, t2);
     v[1] = cadd(t1, t3);
     v[3] = csub(t1, t3);
   }
+  PF_HD static void fwd(float2* v) { run<false>(v); }
 };
 
 // Radix 5 from the pairs x1 +- x4, x2 +- x3:
@@ -227,18 +247,20 @@ struct Dft<17> {
 template <int R1, int R2>
 struct DftComposite {
   static constexpr int R = R1 * R2;
-  PF_HD static void fwd(float2* v) {
+  template <bool INV>
+  PF_HD static void run(float2* v) {
     float2 t[R];
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
       float2 c[R2];
 #pragma unroll
       for (int n2 = 0; n2 < R2; ++n2) c[n2] = v[n1 + R1 * n2];
-      Dft<R2>::fwd(c);
+      if constexpr (INV) dft_inv<R2>(c);
+      else Dft<R2>::fwd(c);
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2) {
         float2 w = wconst<R>(n1 * k2);
-        t[n1 + R1 * k2] = (n1 * k2 == 0) ? c[k2] : cmul(c[k2], w);
+        t[n1 + R1 * k2] = (n1 * k2 == 0) ? c[k2] : (INV ? cmulc(c[k2], w) : cmul(c[k2], w));
       }
     }
 #pragma unroll
@@ -246,11 +268,13 @@ struct DftComposite {
       float2 r[R1];
 #pragma unroll
       for (int n1 = 0; n1 < R1; ++n1) r[n1] = t[n1 + R1 * k2];
-      Dft<R1>::fwd(r);
+      if constexpr (INV) dft_inv<R1>(r);
+      else Dft<R1>::fwd(r);
 #pragma unroll
       for (int k1 = 0; k1 < R1; ++k1) v[k2 + R2 * k1] = r[k1];
     }
   }
+  PF_HD static void fwd(float2* v) { run<false>(v); }
 };
 
 template <>
@@ -259,7 +283,9 @@ struct Dft<6> {
 };
 template <>
 struct Dft<8> {
-  PF_HD static void fwd(float2* v) { DftComposite<2, 4>::fwd(v); }
+  template <bool INV>
+  PF_HD static void run(float2* v) { DftComposite<2, 4>::template run<INV>(v); }
+  PF_HD static void fwd(float2* v) { run<false>(v); }
 };
 template <>
 struct Dft<12> {
@@ -267,7 +293,9 @@ struct Dft<12> {
 };
 template <>
 struct Dft<16> {
-  PF_HD static void fwd(float2* v) { DftComposite<4, 4>::fwd(v); }
+  template <bool INV>
+  PF_HD static void run(float2* v) { DftComposite<4, 4>::template run<INV>(v); }
+  PF_HD static void fwd(float2* v) { run<false>(v); }
 };
 template <>
 struct Dft<10> {
@@ -278,14 +306,23 @@ struct Dft<20> {
   PF_HD static void fwd(float2* v) { DftComposite<4, 5>::fwd(v); }
 };
 
-// Inverse (unnormalised, e^{+2 pi i jk/R}) via conj(DFT(conj(x)))
+// Inverse (unnormalised, e^{+2 pi i jk/R}): sizes built from radix 4 run
+// their butterflies with +i directly; the others as conj(DFT(conj(x))).
+template <int R>
+struct HasRun {
+  static constexpr bool value = (R == 4) || (R == 8) || (R == 16);
+};
 template <int R>
 PF_HD void dft_inv(float2* v) {
+  if constexpr (HasRun<R>::value) {
+    Dft<R>::template run<true>(v);
+  } else {
 #pragma unroll
-  for (int i = 0; i < R; ++i) v[i].y = -v[i].y;
-  Dft<R>::fwd(v);
+    for (int i = 0; i < R; ++i) v[i].y = -v[i].y;
+    Dft<R>::fwd(v);
 #pragma unroll
-  for (int i = 0; i < R; ++i) v[i].y = -v[i].y;
+    for (int i = 0; i < R; ++i) v[i].y = -v[i].y;
+  }
 }
 
 // ---------------------------------------------------------------------------
