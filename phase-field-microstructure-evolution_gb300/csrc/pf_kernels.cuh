@@ -184,20 +184,30 @@ __device__ __forceinline__ float warp_max(float v) {
 // so that IDFT_M(Z') = N z.  Frequencies k and M-k always sit in mirrored
 // runs of the four-step layout, so one thread owns both halves of every pair.
 // ---------------------------------------------------------------------------
-// inverse pre-processing of the pair (k, M-k), 0 < k < M
+// inverse pre-processing of the pair (k, M-k), 0 < k < M.  With
+// s = x_k + conj(x_m), d = x_k - conj(x_m):
+//   z_k = s + i d conj(w_k),   z_m = conj(s) + i (-conj(d)) conj(w_m);
+// the rotated products are formed directly in their final component order so
+// that the sums are packed FP32-pair instructions.
 __device__ __forceinline__ void pre_pair(float2 xk, float2 xm, float2 wk, float2 wm, float2& zk, float2& zm) {
-  const float2 s = cadd(xk, cconj(xm)), d = csub(xk, cconj(xm));
-  zk = cadd(s, cmul_pi(cmulc(d, wk)));
-  // s' = conj(s), d' = -conj(d)
-  const float2 d2 = make_float2(-d.x, d.y);
-  zm = cadd(cconj(s), cmul_pi(cmulc(d2, wm)));
+  const float2 s = __ffma2_rn(xm, make_float2(1.f, -1.f), xk);
+  const float2 d = __ffma2_rn(xm, make_float2(-1.f, 1.f), xk);
+  const float2 ie = make_float2(fmaf(d.x, wk.y, -d.y * wk.x), fmaf(d.x, wk.x, d.y * wk.y));     // i d conj(wk)
+  const float2 ie2 = make_float2(fmaf(-d.y, wm.x, -d.x * wm.y), fmaf(-d.x, wm.x, d.y * wm.y));  // i (-conj d) conj(wm)
+  zk = __fadd2_rn(s, ie);
+  zm = __ffma2_rn(s, make_float2(1.f, -1.f), ie2);
 }
-// forward post-processing of the pair (k, M-k), 0 < k < M, scaled by h = scale/2
+// forward post-processing of the pair (k, M-k), 0 < k < M, scaled by h = scale/2:
+//   x_k = h (s - i d w_k),   x_m = h (conj(s) - i (-conj(d)) w_m),
+// s = z_k + conj(z_m), d = z_k - conj(z_m).
 __device__ __forceinline__ void post_pair(float2 zk, float2 zm, float2 wk, float2 wm, float h, float2& xk, float2& xm) {
-  const float2 s = cadd(zk, cconj(zm)), d = csub(zk, cconj(zm));
-  xk = cscale(cadd(s, cmul_mi(cmul(d, wk))), h);
-  const float2 d2 = make_float2(-d.x, d.y);
-  xm = cscale(cadd(cconj(s), cmul_mi(cmul(d2, wm))), h);
+  const float2 hh = make_float2(h, h);
+  const float2 s = __ffma2_rn(zm, make_float2(1.f, -1.f), zk);
+  const float2 d = __ffma2_rn(zm, make_float2(-1.f, 1.f), zk);
+  const float2 mie = make_float2(fmaf(d.x, wk.y, d.y * wk.x), fmaf(-d.x, wk.x, d.y * wk.y));    // -i d wk
+  const float2 mie2 = make_float2(fmaf(-d.x, wm.y, d.y * wm.x), fmaf(d.x, wm.x, d.y * wm.y));   // -i (-conj d) wm
+  xk = __fmul2_rn(__fadd2_rn(s, mie), hh);
+  xm = __fmul2_rn(__ffma2_rn(s, make_float2(1.f, -1.f), mie2), hh);
 }
 
 // pass A over a runtime number of lines (pitch P, T threads).  A warp takes 32
@@ -231,29 +241,42 @@ __device__ __forceinline__ void passA_rt(float2* buf, int NL, const float2* __re
   }
 }
 
-// Element k of a half spectrum at src + k * stride: read-only global memory
-// (SMEM = false) or a shared-memory staging buffer (SMEM = true).
-template <bool SMEM>
-__device__ __forceinline__ float2 ld_spec(const float2* p) {
-  if constexpr (SMEM) return *p;
-  else return __ldg(p);
+// Where element kx of a line's half spectrum is read from:
+//   SPEC_GLOBAL  src + kx * stride in read-only global memory;
+//   SPEC_SMEM    src + kx * stride in shared memory (a staging buffer);
+//   SPEC_INPLACE the line itself, kx at run kx % N2, element kx / N2 of the
+//                run (x_spec_slot), and kx = M in the pad slot after run 0.
+// In place, the inputs of a run pair are exactly the slots its outputs go
+// to, so every item reads its inputs into registers and overwrites them.
+enum SpecSrc { SPEC_GLOBAL = 0, SPEC_SMEM = 1, SPEC_INPLACE = 2 };
+
+template <int M>
+__device__ __forceinline__ int x_spec_slot(int kx) {
+  constexpr int N1 = Line<M>::N1, N2 = Line<M>::N2;
+  return kx == M ? N1 : (N1 + 1) * (kx % N2) + kx / N2;
+}
+
+template <int SRC, int M>
+__device__ __forceinline__ float2 ld_spec(const float2* src, size_t stride, int kx) {
+  if constexpr (SRC == SPEC_INPLACE) return src[x_spec_slot<M>(kx)];
+  else if constexpr (SRC == SPEC_SMEM) return src[(size_t)kx * stride];
+  else return __ldg(src + (size_t)kx * stride);
 }
 
 // Inverse x transform, first half: read the half spectrum of line (f, yy)
-// (element kx at src + kx * plane) for the run pair `pr`, pre-process,
-// inverse DFT_N1 of each run, store the runs (pass B' output) into the padded
-// line.
-template <int M, bool SMEM = false>
-__device__ __forceinline__ void x_inv_runs(const float2* __restrict__ src, size_t plane, float2* line, int pr,
-                                           const float2* __restrict__ twN) {
+// for the run pair `pr` (from where SRC says), pre-process, inverse DFT_N1 of
+// each run, store the runs (pass B' output) into the padded line.
+template <int M, int SRC = SPEC_GLOBAL>
+__device__ __forceinline__ void x_inv_runs(const float2* src, size_t plane, float2* line, int pr,
+                                           const float2* __restrict__ twN) {  // src may be line (in place)
   constexpr int N1 = Line<M>::N1, N2 = Line<M>::N2;
   if (pr > 0 && 2 * pr < N2) {
     const int ra = pr, rb = N2 - pr;
     float2 a[N1], b[N1];
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) {
-      a[k1] = ld_spec<SMEM>(src + (size_t)(ra + N2 * k1) * plane);
-      b[k1] = ld_spec<SMEM>(src + (size_t)(rb + N2 * k1) * plane);
+      a[k1] = ld_spec<SRC, M>(src, plane, ra + N2 * k1);
+      b[k1] = ld_spec<SRC, M>(src, plane, rb + N2 * k1);
     }
     float2 za[N1], zb[N1];
 #pragma unroll
@@ -271,8 +294,8 @@ __device__ __forceinline__ void x_inv_runs(const float2* __restrict__ src, size_
   } else if (pr == 0) {
     float2 a[N1];
 #pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) a[k1] = ld_spec<SMEM>(src + (size_t)(N2 * k1) * plane);
-    const float2 xM = ld_spec<SMEM>(src + (size_t)M * plane);
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = ld_spec<SRC, M>(src, plane, N2 * k1);
+    const float2 xM = ld_spec<SRC, M>(src, plane, M);
     float2 z[N1];
     z[0] = make_float2(a[0].x + xM.x, a[0].x - xM.x);
 #pragma unroll
@@ -290,7 +313,7 @@ __device__ __forceinline__ void x_inv_runs(const float2* __restrict__ src, size_
     const int ra = N2 / 2;
     float2 a[N1];
 #pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) a[k1] = ld_spec<SMEM>(src + (size_t)(ra + N2 * k1) * plane);
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = ld_spec<SRC, M>(src, plane, ra + N2 * k1);
     float2 z[N1];
 #pragma unroll
     for (int k1 = 0; k1 < N1 / 2; ++k1) {
@@ -654,7 +677,19 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, int c0,
 // ---------------------------------------------------------------------------
 enum XMode { MODE_BULK = 0, MODE_XJ = 1, MODE_IMPORT = 2, MODE_EXPORT = 3 };
 
-template <int NX, int WY, int T, int MODE, bool PHYS = true>
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
+// ASYNC: the tile's half spectra are copied into the line buffer by cp.async
+// (all of them in flight at once, no registers held) in the in-place slot
+// order, and the inverse transform then runs in place; otherwise each item
+// loads its own inputs from global memory.
+template <int NX, int WY, int T, int MODE, bool PHYS = true, bool ASYNC = false>
 __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   constexpr int M = NX / 2;
   using LM = Line<M>;
@@ -684,10 +719,27 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
     // 1. inverse x transform: global half spectrum -> pre-processing -> pass B'
     // a warp covers consecutive (y row, field) lines at one run pair: the
     // global reads are y-contiguous and the line offsets hit distinct banks
-    for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
-      const int l = it % (nF * WY), pr = it / (nF * WY);
-      const int f = l / WY, yy = l - f * WY;
-      x_inv_runs<M>(src + f * fstride + row_off + yy, plane, smem + l * PM, pr, sh.twN);
+    if constexpr (ASYNC) {
+      constexpr int KX = M + 1;
+      // consecutive threads copy consecutive rows of one (field, kx): 64-byte
+      // runs of global memory, destination lines PM apart (distinct banks)
+      for (int it = threadIdx.x; it < nF * KX * WY; it += T) {
+        const int yy = it % WY, r = it / WY, kx = r % KX, f = r / KX;
+        cp_async8(smem + (f * WY + yy) * PM + x_spec_slot<M>(kx),
+                  src + f * fstride + (size_t)kx * plane + row_off + yy);
+      }
+      cp_async_wait_all();
+      __syncthreads();
+      for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
+        const int l = it % (nF * WY), pr = it / (nF * WY);
+        x_inv_runs<M, SPEC_INPLACE>(smem + l * PM, 0, smem + l * PM, pr, sh.twN);
+      }
+    } else {
+      for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
+        const int l = it % (nF * WY), pr = it / (nF * WY);
+        const int f = l / WY, yy = l - f * WY;
+        x_inv_runs<M>(src + f * fstride + row_off + yy, plane, smem + l * PM, pr, sh.twN);
+      }
     }
     __syncthreads();
     passA_rt<M, PM, T, true>(smem, nF * WY, sh.twM);
@@ -807,7 +859,7 @@ __global__ void __launch_bounds__(T, MINB) x_pass_tma_kernel(const RunParams* __
     for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
       const int l = it % (nF * WY), pr = it / (nF * WY);
       const int f = l / WY, yy = l - f * WY;
-      x_inv_runs<M, true>(stage + (size_t)f * G::FSTRIDE + yy, WY, smem + l * PM, pr, sh.twN);
+      x_inv_runs<M, SPEC_SMEM>(stage + (size_t)f * G::FSTRIDE + yy, WY, smem + l * PM, pr, sh.twN);
     }
     __syncthreads();
     if (threadIdx.x == 0 && tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x);  // staging is free again

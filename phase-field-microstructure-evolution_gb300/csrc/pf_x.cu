@@ -44,6 +44,24 @@ static int addtma(XKernels* out, int n) {
   return n;
 }
 
+// every mode with the tile's spectra copied in by cp.async and transformed in
+// place (PHYS: the bulk walk over physical slots)
+template <int NX, int WY, int T, bool PHYS = false>
+static int addas(XKernels* out, int n) {
+  if (n >= kMaxVariants) return n;
+  XKernels& k = out[n];
+  k.bulk = x_pass_kernel<NX, WY, T, MODE_BULK, PHYS, true>;
+  k.xj = x_pass_kernel<NX, WY, T, MODE_XJ, PHYS, true>;
+  k.imp = x_pass_kernel<NX, WY, T, MODE_IMPORT>;
+  k.exp = x_pass_kernel<NX, WY, T, MODE_EXPORT, PHYS, true>;
+  k.wy = WY;
+  k.threads = T;
+  k.cl = 0;
+  k.tma = 0;
+  k.bulk_smem = nullptr;
+  return n + 1;
+}
+
 // bulk pass walking the logical cells (for comparison with the physical-slot walk)
 template <int NX, int WY, int T>
 static int addlog(XKernels* out, int n) {
@@ -89,11 +107,13 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = addtma<128, 8, 512>(out, n); n = addtma<128, 8, 256>(out, n);
       n = addlog<128, 8, 256>(out, n);
       n = addtma<128, 4, 256, 3>(out, n); n = addtma<128, 4, 384, 2>(out, n);
+      n = addas<128, 8, 256>(out, n); n = addas<128, 8, 256, true>(out, n); n = addas<128, 4, 256>(out, n);
       break;
     case 256:
       n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n);
       n = addcl<256, 4, 256>(out, n); n = addcl<256, 4, 512>(out, n);
       n = addtma<256, 4, 512>(out, n); n = addtma<256, 2, 512>(out, n);
+      n = addas<256, 4, 512>(out, n); n = addas<256, 2, 256>(out, n);
       break;
     default: break;
   }
