@@ -485,10 +485,10 @@ static bool xj_ok(pf_batch* b, const XKernels& k) {
 }
 
 static void describe_variants(pf_batch* b) {
-  char buf[160];
-  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d%s yz:cluster=%d,threads=%d xj:wy=%d,threads=%d", b->xk.wy,
-           b->xk.threads, b->xk.cl ? ",cluster=2" : (b->xk.tma ? ",tma" : ""), b->yk.cluster, b->yk.threads,
-           b->xjk.wy, b->xjk.threads);
+  char buf[256];
+  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d%s%s yz:cluster=%d,threads=%d%s xj:wy=%d,threads=%d%s", b->xk.wy,
+           b->xk.threads, b->xk.cl ? ",cluster=2" : (b->xk.tma ? ",tma" : ""), b->xk.tag, b->yk.cluster,
+           b->yk.threads, b->yk.inpl ? ",in-place" : "", b->xjk.wy, b->xjk.threads, b->xjk.tag);
   b->variant = buf;
 }
 

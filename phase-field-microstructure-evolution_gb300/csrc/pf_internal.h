@@ -18,6 +18,7 @@ struct XKernels {
   int cl = 0;   // 2: the bulk kernel runs as clusters of two CTAs sharing the fields (x_pass_cl_kernel)
   int tma = 0;  // > 0: the bulk kernel is the persistent TMA-staged x_pass_tma_kernel, at most this many CTAs per SM
   size_t (*bulk_smem)(int nF) = nullptr;  // its dynamic shared memory (cluster and TMA variants)
+  const char* tag = "";  // how the tile is loaded and walked, for reports
 };
 
 // ... and of the yz pass (all three modes).
@@ -26,6 +27,7 @@ struct YZKernels {
   int cluster;   // CTAs per plane
   int threads;   // threads per CTA
   size_t smem;   // dynamic shared memory per CTA
+  int inpl = 0;  // 1: the cluster exchanges the plane in place (one buffer per CTA)
 };
 
 // Variant lists: each translation unit appends the variants it compiled for a

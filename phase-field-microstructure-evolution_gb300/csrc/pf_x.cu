@@ -18,6 +18,7 @@ static int add(XKernels* out, int n) {
   k.cl = 0;
   k.tma = 0;
   k.bulk_smem = nullptr;
+  k.tag = "";
   return n + 1;
 }
 
@@ -59,6 +60,7 @@ static int addas(XKernels* out, int n) {
   k.cl = 0;
   k.tma = 0;
   k.bulk_smem = nullptr;
+  k.tag = "";
   return n + 1;
 }
 
@@ -68,6 +70,7 @@ static int addlog(XKernels* out, int n) {
   if (n >= kMaxVariants) return n;
   n = add<NX, WY, T>(out, n);
   out[n - 1].bulk = x_pass_kernel<NX, WY, T, MODE_BULK, false>;
+  out[n - 1].tag = ",logical";
   return n;
 }
 
@@ -108,6 +111,8 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = addlog<128, 8, 256>(out, n);
       n = addtma<128, 4, 256, 3>(out, n); n = addtma<128, 4, 384, 2>(out, n);
       n = addas<128, 8, 256>(out, n); n = addas<128, 8, 256, true>(out, n); n = addas<128, 4, 256>(out, n);
+      // many rows for the one-field xj pass (its bulk mode does not fit: never chosen for the bulk pass)
+      n = add<128, 32, 256>(out, n);
       break;
     case 256:
       n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n);

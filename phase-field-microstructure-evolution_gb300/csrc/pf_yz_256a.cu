@@ -14,6 +14,7 @@ static int add(YZKernels* out, int n) {
   k.cluster = C;
   k.threads = T;
   k.smem = INPL ? YZ<NY, NZ, C>::SMEM_INPL : YZ<NY, NZ, C>::SMEM;
+  k.inpl = INPL ? 1 : 0;
   return n + 1;
 }
 
