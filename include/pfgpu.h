@@ -120,6 +120,19 @@ int pf_batch_step(pf_batch* b, int nsteps, pf_diag* diag);
 int pf_batch_get_fields(pf_batch* b, int run, double* phi_aos, double* con);
 int pf_batch_destroy(pf_batch* b);
 
+/* ---- a run's error against the FP64 GPU path -------------------------------
+ * The same start stepped nsteps times on the fused FP32 path and on the plain
+ * FP64 path (cuFFT + one kernel per phase of src/var_diff.f90:556-1050, held
+ * to the FP64 CPU restatement at 1e-10 by the tests); the fields are compared
+ * on the device: max-abs and L2 difference relative to the FP64 fields'
+ * max-abs and L2 norm, for all order parameters together and for c.  Holds
+ * both runs' memory while it works. */
+typedef struct pf_error_report {
+  int steps, pad;
+  double phi_max_abs_rel, phi_l2_rel, c_max_abs_rel, c_l2_rel;
+} pf_error_report;
+int pf_check_fp64(const pf_config* cfg, const double* phi_aos, const double* con, int nsteps, pf_error_report* out);
+
 /* ---- serving: continuous batching of independent runs on one GPU --------
  * The reference runs a parameter study as one SLURM job per run
  * (tests/run_phase_sim.py:130-172); a pf_server takes the runs as requests in
@@ -258,7 +271,8 @@ int pf_diag_fields_noalloc(const pf_config* cfg, const float* fields, pf_diag* o
  * continue on following lines.  Lines after `start` may hold key=value pairs
  * that the reference ignores: seed, n_grains, amp_phi, amp_c, c0 (for the
  * 'noise' and 'voronoi' starts), mobility (reference|c1mc), precision (32|64),
- * microstructure (the 'polycryst' file; the reference opens a fixed path). */
+ * microstructure (the 'polycryst' file; the reference opens a fixed path),
+ * check_fp64 (steps of the start compared with the FP64 GPU path). */
 typedef struct pf_input {
   int nrun, ppt_int;                       /* bits 0, 1 */
   int ppt_rad[3], N_step, ifreq;           /* bits 2, 3, 4 */
@@ -278,6 +292,7 @@ typedef struct pf_input {
   int seed, n_grains, mobility, precision; /* precision 0: fused FP32 where supported */
   double amp_phi, amp_c, c0;
   char microstructure[256];
+  int check_fp64; /* > 0: report the run's error against the FP64 GPU path after this many steps */
 } pf_input;
 
 /* Message of the last failed pf_read_input / pf_*data_save / pf_ic_* call. */

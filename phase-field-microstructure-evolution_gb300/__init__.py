@@ -16,7 +16,7 @@ from .pfgpu import (Batch, Config, Diag, PFError, Ran2, Run, load_library, libra
                     ic_polycryst, insert_precipitates, format_e, format_summary, format_list_int,
                     format_list_real, driver_path, VoxelCounts, AnalysisOut, analyze_fields, analyze_run,
                     write_vtk, paraview_path, sweep, sweep_path, variant_counts, Server, ServerConfig,
-                    RequestTimes, Pool, place_units, pick_device, PF_EBUSY, PF_REQ_QUEUED, PF_REQ_RUNNING, PF_REQ_DONE, PF_REQ_FAILED)
+                    RequestTimes, Pool, place_units, pick_device, check_fp64, ErrorReport, PF_EBUSY, PF_REQ_QUEUED, PF_REQ_RUNNING, PF_REQ_DONE, PF_REQ_FAILED)
 
 
 def build(force: bool = False, verbose: bool = False):

@@ -229,6 +229,7 @@ int pf_read_input(const char* path, int nprocs, pf_input* in) {
   in->c0 = 0.5;
   in->n_grains = 8;
   snprintf(in->microstructure, sizeof in->microstructure, "mc_ivar_fin");
+  in->check_fp64 = 0;
   std::vector<std::string> v;
   auto take_i = [&](int idx, int* dst, int bit) {
     if ((int)v.size() > idx) { *dst = inum(v[idx]); in->set_mask |= (1ull << bit); }
@@ -287,6 +288,7 @@ int pf_read_input(const char* path, int nprocs, pf_input* in) {
       else if (k == "mobility") in->mobility = (val == "c1mc") ? PF_MOB_C1MC : PF_MOB_REFERENCE;
       else if (k == "precision") in->precision = inum(val);
       else if (k == "microstructure") snprintf(in->microstructure, sizeof in->microstructure, "%s", val.c_str());
+      else if (k == "check_fp64") in->check_fp64 = inum(val);
     }
   }
   if (!(in->set_mask & (1ull << 11)) || in->Nx < 1 || in->Ny < 1 || in->Nz < 1 || in->var < 1)

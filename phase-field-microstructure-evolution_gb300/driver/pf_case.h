@@ -115,6 +115,18 @@ struct Case {
     if (in.ifreq < 1) throw Error(2, "ifreq must be >= 1");
   }
 
+  // check_fp64=N: the start stepped N times on the fused and the FP64 GPU
+  // paths, the run's error reported on the log (fused-path runs only)
+  void report_fp64_check() {
+    if (in.check_fp64 <= 0 || cfg.precision != PF_FP32_FUSED) return;
+    pf_error_report rep;
+    if (pf_check_fp64(&cfg, phi.data(), con.data(), in.check_fp64, &rep) != PF_OK)
+      throw Error(2, std::string("pf_check_fp64: ") + pf_last_error());
+    fprintf(log, " fp64 check: %d steps, phi max-abs rel %.3e l2 rel %.3e, c max-abs rel %.3e l2 rel %.3e\n",
+            rep.steps, rep.phi_max_abs_rel, rep.phi_l2_rel, rep.c_max_abs_rel, rep.c_l2_rel);
+    fflush(log);
+  }
+
   std::string path_of(const char* p) const {
     if (base.empty() || p[0] == '/') return p;
     return base + "/" + p;

@@ -227,6 +227,7 @@ int main(int argc, char** argv) {
               c.in.var, c.in.N_step, c.cfg.precision == PF_FP64_PLAIN ? "FP64 cuFFT" : "fused FP32");
       c.open_outputs();
       c.make_start();
+      c.report_fp64_check();
     } catch (const pfcase::Error& e) {
       fail_member(m, e.code, e.what());
       continue;

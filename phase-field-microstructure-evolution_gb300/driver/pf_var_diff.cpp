@@ -19,7 +19,8 @@
 // non-finite values stops the run with exit status 3 after writing its
 // records; 'polycryst' reads the `microstructure=` file (default mc_ivar_fin
 // in the working directory) instead of the reference's fixed path; 'noise'
-// and 'voronoi' are extra starts driven by the key=value lines.
+// and 'voronoi' are extra starts driven by the key=value lines; check_fp64=N
+// prints the run's error against the FP64 GPU path after N steps of its start.
 #include <chrono>
 #include <cstdio>
 #include <string>
@@ -43,6 +44,7 @@ int main(int argc, char** argv) {
     fflush(stdout);
     c.open_outputs();
     c.make_start();
+    c.report_fp64_check();
     pfcase::check(pf_create(&c.cfg, &run), "pf_create");
     pfcase::check(pf_set_fields(run, c.phi.data(), c.con.data()), "pf_set_fields");
     // time loop (src/var_diff.f90:473-1158), advanced in chunks that end at

@@ -29,7 +29,7 @@ EXPORTED = (
     "pf_ic_polycryst", "pf_insert_precipitates", "pf_format_e", "pf_format_summary", "pf_format_list_int",
     "pf_format_list_real", "pf_analyze_fields", "pf_analyze_run", "pf_write_vtk_real", "pf_write_vtk_int",
     "pf_server_create", "pf_server_submit", "pf_server_poll", "pf_server_wait", "pf_server_destroy",
-    "pf_server_last_error", "pf_device_count", "pf_run_work", "pf_pick_device", "pf_place_units", "pf_pool_create", "pf_pool_devices",
+    "pf_server_last_error", "pf_check_fp64", "pf_device_count", "pf_run_work", "pf_pick_device", "pf_place_units", "pf_pool_create", "pf_pool_devices",
     "pf_pool_submit", "pf_pool_wait", "pf_pool_destroy", "pf_pool_last_error",
 )
 
@@ -84,11 +84,17 @@ class Input(C.Structure):
         ("set_mask", C.c_ulonglong),
         ("seed", C.c_int), ("n_grains", C.c_int), ("mobility_code", C.c_int), ("precision", C.c_int),
         ("amp_phi", C.c_double), ("amp_c", C.c_double), ("c0", C.c_double), ("microstructure", C.c_char * 256),
+        ("check_fp64", C.c_int),
     ]
 
     @property
     def mobility(self):
         return "c1mc" if self.mobility_code == PF_MOB_C1MC else "reference"
+
+
+class ErrorReport(C.Structure):
+    _fields_ = [("steps", C.c_int), ("pad", C.c_int), ("phi_max_abs_rel", C.c_double), ("phi_l2_rel", C.c_double),
+                ("c_max_abs_rel", C.c_double), ("c_l2_rel", C.c_double)]
 
 
 class ServerConfig(C.Structure):
@@ -191,6 +197,7 @@ def load_library(build_if_missing: bool = True) -> C.CDLL:
         "pf_server_destroy": (C.c_int, [C.c_void_p]),
         "pf_server_last_error": (C.c_char_p, []),
         "pf_device_count": (C.c_int, []),
+        "pf_check_fp64": (C.c_int, [P(Config), dp, dp, C.c_int, P(ErrorReport)]),
         "pf_run_work": (C.c_double, [P(Config), C.c_int]),
         "pf_pick_device": (C.c_int, [dp, C.c_int]),
         "pf_place_units": (C.c_int, [dp, C.c_int, C.c_int, ip, dp]),
@@ -341,6 +348,19 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def check_fp64(p, phi: np.ndarray, con: np.ndarray, nsteps: int, device: int = 0) -> dict:
+    """The run's error against the FP64 GPU path after nsteps steps of the
+    start (phi[ivar,z,y,x], con[z,y,x]): max-abs and L2 differences relative to
+    the FP64 fields' max-abs and L2 norms (pf_check_fp64)."""
+    lib = load_library()
+    cfg = make_config(p, PF_FP32_FUSED, device)
+    a = to_aos(phi)
+    c = np.ascontiguousarray(con, dtype=np.float64)
+    rep = ErrorReport()
+    _check(lib.pf_check_fp64(C.byref(cfg), _dp(a), _dp(c), int(nsteps), C.byref(rep)))
+    return {k: getattr(rep, k) for k, _ in rep._fields_ if k != "pad"}
 
 
 def _ic_buffers(p, pinned: bool):
