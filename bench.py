@@ -620,8 +620,8 @@ def run_serve(args):
     per visible GPU) against serial execution of the same requests.  The
     request properties come from the same ran_2 draws at every rate; only the
     arrival times scale with 1/rate.  Serial: each request's service time alone
-    (pf_create / pf_set_fields / pf_step / pf_get_fields, measured once),
-    replayed as a FIFO single server at each rate's arrival times."""
+    (pf_create / pf_set_fields / pf_step / pf_get_fields / pf_destroy, measured
+    once), replayed as a FIFO single server at each rate's arrival times."""
     import torch
 
     torch.cuda.set_device(0)
@@ -641,13 +641,13 @@ def run_serve(args):
     # serial service times, measured once
     service = []
     for (_, p, steps, _, _), (phi, con) in zip(base, starts):
-        run = pkg.Run(p)
         tb = time.perf_counter()
+        run = pkg.Run(p)
         run.set_fields(phi, con)
         run.step(steps, raise_nonfinite=False)
         run.get_fields()
-        service.append(time.perf_counter() - tb)
         run.close()
+        service.append(time.perf_counter() - tb)
     n = len(base)
     work = sum(p.Nx * p.Ny * p.Nz * p.var * steps for (_, p, steps, _, _) in base)
     per_rate = []
@@ -682,8 +682,8 @@ def run_serve(args):
             "config": {"workload": f"served stream: {n} requests per rate, Poisson rates {rates}/s, grids 32-256, "
                                    f"P 4-16, 100-5000 steps (config 4)", "max_active": args.max_active},
             "rates": per_rate,
-            "serial_what": "each request alone (pf_create/pf_set_fields/pf_step/pf_get_fields), service times "
-                           "measured once, FIFO single server at each rate's arrival times"}
+            "serial_what": "each request alone (pf_create/pf_set_fields/pf_step/pf_get_fields/pf_destroy), "
+                           "service times measured once, FIFO single server at each rate's arrival times"}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -139,9 +139,10 @@ int pf_check_fp64(const pf_config* cfg, const double* phi_aos, const double* con
  * one process.  A worker thread admits queued requests as the resident runs
  * leave room in the device-memory budget and in max_active; waiting requests
  * of the same grid, var and mobility class are admitted together as one
- * batch, every batch steps on its own stream, and batches of different shapes
- * overlap on the device.  A run leaves as soon as its own step count is
- * reached.  Results do not depend on what else is running (per-run
+ * batch and every batch steps on its own stream.  Batches that fill the GPU by
+ * themselves (runs x cells x (var+1) >= 2^24) take turns, oldest admitted
+ * first; smaller batches run beside them on high-priority streams.  A run
+ * leaves as soon as its own step count is reached.  Results do not depend on what else is running (per-run
  * reductions, no shared state).  Fused FP32 path only. */
 typedef struct pf_server pf_server;
 typedef struct pf_server_config {

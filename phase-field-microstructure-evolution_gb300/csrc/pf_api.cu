@@ -1050,6 +1050,19 @@ int pf_batch_c_mean(pf_batch* b, int run, double* re_im) {
 }
 // Length of a batch's per-run record ring (steps whose records stay readable).
 int pf_batch_ring(pf_batch* b) { return b ? b->ring : 0; }
+// Give the batch's stream the device's highest scheduling priority (before
+// any step is enqueued on it): its launches then take SMs ahead of
+// lower-priority work as SMs free up.
+int pf_batch_prioritize(pf_batch* b) {
+  if (!b) return fail(PF_EINVAL, "null batch");
+  PF_CUDA(cudaSetDevice(b->device));
+  PF_CUDA(cudaStreamSynchronize(b->stream));
+  cudaStream_t s = nullptr;
+  PF_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, b->prio_hi));
+  cudaStreamDestroy(b->stream);
+  b->stream = s;
+  return PF_OK;
+}
 // Number of compiled x-pass and yz-pass variants of a grid (the index range
 // of PFGPU_X_VARIANT / PFGPU_YZ_VARIANT).
 void pf_variant_counts(int nx, int ny, int nz, int* nxv, int* nyzv) {

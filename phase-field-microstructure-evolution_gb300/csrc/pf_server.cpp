@@ -11,8 +11,10 @@
 //     (one set of launches per step for all of them);
 //   * every resident batch has its own stream and captured step graph; the
 //     worker keeps up to two chunks of steps queued on each batch and tops
-//     them up as they complete, so batches of different shapes overlap on the
-//     device, and the device has work while the worker admits new requests;
+//     them up as they complete, so the device has work while the worker
+//     admits new requests; batches that fill the GPU by themselves take turns
+//     (oldest admitted first), smaller batches overlap with them on
+//     high-priority streams;
 //   * a run leaves as soon as its own step count is reached (its fields and
 //     last record are copied out; a batch is freed when all its runs left).
 // Each run computes exactly what it computes alone: the same kernels, per-run
@@ -43,6 +45,7 @@ size_t pf_batch_bytes(const pf_config* c, int nruns);
 int pf_batch_steps_done(pf_batch* b, int run);
 int pf_batch_records(pf_batch* b, int run, int first, int n, pf_diag* out);
 int pf_batch_ring(pf_batch* b);
+int pf_batch_prioritize(pf_batch* b);
 }
 
 namespace {
@@ -79,9 +82,17 @@ constexpr int kRing = 1024;   // per-run record ring of a batch (pf_batch_ring)
 // once, since the newest chunk writes its slots while the oldest one's are
 // copied out.
 constexpr int kMaxChunk = kRing / kInFlight;
+// A batch whose step touches at least this many cell-fields (runs x cells x
+// (var + 1)) keeps the whole GPU busy by itself: such batches do not gain
+// from running side by side, they only evict each other's data from L2 and
+// fragment the SMs, so they take turns (oldest admitted first), while the
+// smaller batches run beside them on high-priority streams.
+constexpr double kHeavyCellFields = 16777216.0;
 
 struct Active {
   pf_batch* b = nullptr;
+  bool heavy = false;      // fills the GPU on its own (run one at a time, oldest first)
+  long long seq = 0;       // admission order
   std::vector<std::shared_ptr<Request>> runs;
   std::vector<bool> left;  // run finished and copied out
   size_t bytes = 0;
@@ -104,6 +115,7 @@ struct pf_server {
   std::thread worker;
   std::vector<Active> active;
   int resident = 0;
+  long long next_seq = 0;
 };
 
 namespace {
@@ -188,6 +200,9 @@ void admit(pf_server* s) {
     a.runs = group;
     a.left.assign(group.size(), false);
     a.bytes = pf_batch_bytes(&cfgs[0], (int)cfgs.size());
+    a.heavy = (double)cfgs.size() * cfgs[0].nx * cfgs[0].ny * cfgs[0].nz * (cfgs[0].var + 1) >= kHeavyCellFields;
+    a.seq = s->next_seq++;
+    if (!a.heavy) pf_batch_prioritize(a.b);  // best effort: default priority if it fails
     {
       std::lock_guard<std::mutex> lk(s->mu);
       const auto now = Clock::now();
@@ -261,6 +276,11 @@ void worker_loop(pf_server* s) {
       }
     }
     bool progressed = false;
+    long long oldest_heavy = -1;  // the heavy batch whose turn it is
+    for (const Active& a : s->active)
+      if (a.heavy && !std::all_of(a.left.begin(), a.left.end(), [](bool v) { return v; }) &&
+          (oldest_heavy < 0 || a.seq < oldest_heavy))
+        oldest_heavy = a.seq;
     for (Active& a : s->active) {
       // completed chunks, oldest first
       while (!a.flight.empty() && cudaEventQuery(a.flight.front().ev) != cudaErrorNotReady) {
@@ -274,7 +294,7 @@ void worker_loop(pf_server* s) {
         if (a.flight.empty()) fail_rest(s, a, PF_EINVAL, "server destroyed before the run finished");
         continue;
       }
-      while ((int)a.flight.size() < kInFlight) {
+      while ((int)a.flight.size() < kInFlight && (!a.heavy || a.seq == oldest_heavy)) {
         const int n = next_chunk(s, a);
         if (n <= 0) break;
         Chunk c;
