@@ -119,6 +119,8 @@ static int build_tables(int Nx, int Ny, int Nz, DevTables& t) {
   Shape& s = t.sh;
   s.Nx = Nx; s.Ny = Ny; s.Nz = Nz; s.Kx = Kx;
   s.plane0 = 0;
+  s.pref_x = 0;
+  s.pref_yz = 0;
   s.twM = (const float2*)(b + off_tw[0]);
   s.twN = (const float2*)(b + off_tw[1]);
   s.twY = (const float2*)(b + off_tw[2]);
@@ -393,15 +395,9 @@ __global__ void fill_kernel(float* p, size_t n, float v0, float v1) {
 static std::mutex g_tune_mu;
 static std::map<std::string, std::tuple<int, int, int>> g_tune_cache;  // x, yz, xj variant
 
-static bool yz_ok(pf_batch* b, const YZKernels& k) {
-  if (k.smem > kMaxSmem) return false;
-  for (KernelFn f : {k.main, k.c2, k.imp}) {
-    if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem) != cudaSuccess)
-      return false;
-    if (k.cluster > 8 &&
-        cudaFuncSetAttribute((const void*)f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
-      return false;
-  }
+// Clusters of a yz-pass variant resident on the device at once (0: it cannot
+// be scheduled).
+static int yz_clusters(pf_batch* b, const YZKernels& k) {
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -414,9 +410,21 @@ static bool yz_ok(pf_batch* b, const YZKernels& k) {
   cfg.attrs = at;
   cfg.numAttrs = 1;
   int ncl = 0;
-  cudaError_t e = cudaOccupancyMaxActiveClusters(&ncl, (const void*)k.main, &cfg);
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&ncl, (const void*)k.main, &cfg);
   cudaGetLastError();
-  return e == cudaSuccess && ncl >= 1;
+  return e == cudaSuccess ? ncl : 0;
+}
+
+static bool yz_ok(pf_batch* b, const YZKernels& k) {
+  if (k.smem > kMaxSmem) return false;
+  for (KernelFn f : {k.main, k.c2, k.imp}) {
+    if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem) != cudaSuccess)
+      return false;
+    if (k.cluster > 8 &&
+        cudaFuncSetAttribute((const void*)f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+      return false;
+  }
+  return yz_clusters(b, k) >= 1;
 }
 
 // Dynamic shared memory a kernel may use is a per-function setting shared by
@@ -486,9 +494,10 @@ static bool xj_ok(pf_batch* b, const XKernels& k) {
 
 static void describe_variants(pf_batch* b) {
   char buf[256];
-  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d%s%s yz:cluster=%d,threads=%d%s xj:wy=%d,threads=%d%s", b->xk.wy,
+  snprintf(buf, sizeof buf, "x:wy=%d,threads=%d%s%s yz:cluster=%d,threads=%d%s%s xj:wy=%d,threads=%d%s", b->xk.wy,
            b->xk.threads, b->xk.cl ? ",cluster=2" : (b->xk.tma ? ",tma" : ""), b->xk.tag, b->yk.cluster,
-           b->yk.threads, b->yk.inpl ? ",in-place" : "", b->xjk.wy, b->xjk.threads, b->xjk.tag);
+           b->yk.threads, b->yk.inpl ? ",in-place" : "", b->yk.pref ? ",L2-prefetch" : "", b->xjk.wy,
+           b->xjk.threads, b->xjk.tag);
   b->variant = buf;
 }
 
@@ -530,6 +539,18 @@ static void apply_variants(pf_batch* b, const XKernels& xk, const YZKernels& yk)
   }
   b->tab.sh.nblk_x = b->Nz * (b->Ny / xk.wy);
   b->tab.sh.nblk_yz = yk.cluster * b->nF * b->Kx;
+  // L2 prefetch distances: the CTAs resident at once
+  b->tab.sh.pref_x = 0;
+  if (xk.pref) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)xk.bulk, xk.threads, b->smem_bulk) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      occ = 0;
+    }
+    b->tab.sh.pref_x = occ * b->nsm;
+  }
+  b->tab.sh.pref_yz = yk.pref ? yz_clusters(b, yk) * yk.cluster : 0;
   apply_xj(b, xk);
 }
 

@@ -19,6 +19,7 @@ struct XKernels {
   int tma = 0;  // > 0: the bulk kernel is the persistent TMA-staged x_pass_tma_kernel, at most this many CTAs per SM
   size_t (*bulk_smem)(int nF) = nullptr;  // its dynamic shared memory (cluster and TMA variants)
   const char* tag = "";  // how the tile is loaded and walked, for reports
+  int pref = 0;          // 1: the bulk kernel prefetches the next generation's tiles into L2 (Shape::pref_x)
 };
 
 // ... and of the yz pass (all three modes).
@@ -28,12 +29,13 @@ struct YZKernels {
   int threads;   // threads per CTA
   size_t smem;   // dynamic shared memory per CTA
   int inpl = 0;  // 1: the cluster exchanges the plane in place (one buffer per CTA)
+  int pref = 0;  // 1: the main kernel prefetches the next generation's planes into L2 (Shape::pref_yz)
 };
 
 // Variant lists: each translation unit appends the variants it compiled for a
 // shape to `out` (room for kMaxVariants entries) and returns the new count.  The first variant of a shape is its
 // default; the run-creation autotuner times the others.
-constexpr int kMaxVariants = 16;
+constexpr int kMaxVariants = 20;
 int x_variants_a(int nx, XKernels* out, int n);
 int x_variants_r5(int nx, XKernels* out, int n);
 int yz_variants_small(int ny, int nz, YZKernels* out, int n);

@@ -86,25 +86,12 @@ struct Shape {
   int nblk_x;   // blocks of the x pass per run
   int nblk_yz;  // blocks of the yz pass per run
   int plane0;   // first (field, kx) plane of a yz-pass launch (a launch may cover a subset)
+  // L2 prefetch distance in CTAs of the x / yz pass variants that prefetch:
+  // the CTAs resident at once, so that CTA b fetches into L2 what CTA b + pref
+  // (which starts about when b ends) will read; 0: none
+  int pref_x, pref_yz;
 };
 
-// ---------------------------------------------------------------------------
-// Block reductions
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-// FP32 warp sum for the yz pass's f_int partials (32 FP32 thread sums); the
-// per-warp results are added in FP64 per block and across blocks.  FP64
-// arithmetic is scarce on this part, FP32 shuffles are not.  (The x pass keeps
-// FP64 shuffles for its partials: with FP32 ones that kernel measured slower.)
-__device__ __forceinline__ float warp_sumf(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 // ---------------------------------------------------------------------------
 // Compensated sums for the mass of c (src/var_diff.f90:1076-1102).  A thread
 // keeps its running sum as an unevaluated FP32 pair hi + lo updated with
@@ -684,12 +671,27 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
+// Prefetch [p, p + bytes) into L2 (cp.async.bulk.prefetch): no registers, no
+// completion to wait for.  p 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+// Prefetch [p, p + bytes) into L2 in chunks of at most 4 KB, one per lane of
+// the calling warp.
+__device__ __forceinline__ void prefetch_l2_warp(const void* p, size_t bytes, int lane) {
+  constexpr size_t CH = 4096;
+  for (size_t o = (size_t)lane * CH; o < bytes; o += 32 * CH)
+    prefetch_l2(static_cast<const char*>(p) + o, (unsigned)(bytes - o < CH ? bytes - o : CH));
+}
 
 // ASYNC: the tile's half spectra are copied into the line buffer by cp.async
 // (all of them in flight at once, no registers held) in the in-place slot
 // order, and the inverse transform then runs in place; otherwise each item
-// loads its own inputs from global memory.
-template <int NX, int WY, int T, int MODE, bool PHYS = true, bool ASYNC = false>
+// loads its own inputs from global memory.  PREF (with ASYNC, bulk mode): once
+// its own spectra have arrived, the CTA prefetches into L2 the spectra of tile
+// blockIdx.x + sh.pref_x, which starts about when this one ends, so that the
+// HBM reads of the next generation of CTAs overlap this one's arithmetic.
+template <int NX, int WY, int T, int MODE, bool PHYS = true, bool ASYNC = false, bool PREF = false>
 __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   constexpr int M = NX / 2;
   using LM = Line<M>;
@@ -730,6 +732,17 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
       }
       cp_async_wait_all();
       __syncthreads();
+      if constexpr (PREF && MODE == MODE_BULK) {
+        const int t2 = (int)blockIdx.x + sh.pref_x;
+        if (sh.pref_x > 0 && t2 < (int)gridDim.x) {
+          const int z2 = t2 / ny_tiles;
+          const size_t row2 = (size_t)z2 * sh.Ny + (size_t)(t2 - z2 * ny_tiles) * WY;
+          for (int it = threadIdx.x; it < nF * KX; it += T) {
+            const int kx = it % KX, f = it / KX;
+            prefetch_l2(src + f * fstride + (size_t)kx * plane + row2, WY * 8);
+          }
+        }
+      }
       for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
         const int l = it % (nF * WY), pr = it / (nF * WY);
         x_inv_runs<M, SPEC_INPLACE>(smem + l * PM, 0, smem + l * PM, pr, sh.twN);
@@ -1324,7 +1337,10 @@ __device__ __forceinline__ void passB(float2* buf) {
   }
 }
 
-template <int NY, int NZ, int C, int T, int MODE, bool INPL = false>
+// PREF (main mode): before its k-space update the CTA prefetches into L2 the
+// D~ rows and k-space block that CTA blockIdx.x + sh.pref_yz (a multiple of C:
+// the same cluster rank, about one generation of resident CTAs later) reads.
+template <int NY, int NZ, int C, int T, int MODE, bool INPL = false, bool PREF = false>
 __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = YZ<NY, NZ, C>;
   using LY = Line<NY>;
@@ -1382,6 +1398,20 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   __syncthreads();
   passA<NZ, G::LB, G::PZ, T, false>(UB, sh.twZ);
   __syncthreads();
+  if constexpr (PREF && MODE == YZ_MAIN) {
+    const int b2 = (int)blockIdx.x + sh.pref_yz;
+    if (sh.pref_yz > 0 && b2 < (int)gridDim.x && threadIdx.x < 64) {
+      const int p2 = sh.plane0 + b2 / C, f2 = p2 / Kx, kx2 = p2 - f2 * Kx, r2 = b2 % C;
+      const size_t poff2 = f2 * fstride + kx2 * plane_elems;
+      const int lane = threadIdx.x & 31;
+      if (threadIdx.x < 32) {
+        prefetch_l2_warp(rp.D + poff2 + (size_t)r2 * G::LA * NY, (size_t)G::LA * NY * 8, lane);
+      } else {
+        for (int k1 = lane; k1 < N1z; k1 += 32)
+          prefetch_l2(rp.Sk + poff2 + (size_t)k1 * NY * N2z + (size_t)r2 * G::LB * N2z, G::LB * N2z * 8);
+      }
+    }
+  }
 
   // 2. last forward z pass, pointwise k-space update, first inverse z pass,
   //    fused per run of N1z positions
@@ -1529,7 +1559,10 @@ __device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
   }
 }
 
-template <int NY, int NZ, int T, int MODE, bool RAWP = false>
+// PREF (main mode): before its k-space update the CTA prefetches into L2 the
+// D~ and k-space planes of CTA blockIdx.x + sh.pref_yz (about one generation
+// of resident CTAs later).
+template <int NY, int NZ, int T, int MODE, bool RAWP = false, bool PREF = false>
 __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using LY = Line<NY>;
   using LZ = Line<NZ>;
@@ -1581,6 +1614,13 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   __syncthreads();
   colA<NY, NZ, T, false, RAWP>(U, sh.twZ);
   __syncthreads();
+  if constexpr (PREF && MODE == YZ_MAIN) {
+    const int p2 = p + sh.pref_yz;
+    if (sh.pref_yz > 0 && (int)blockIdx.x + sh.pref_yz < (int)gridDim.x && threadIdx.x < 64) {
+      const size_t poff2 = (size_t)p2 * plane_elems;  // (f2 Kx + kx2) planes
+      prefetch_l2_warp((threadIdx.x < 32 ? rp.D : rp.Sk) + poff2, plane_elems * 8, threadIdx.x & 31);
+    }
+  }
 
   // 2. last forward z pass, pointwise k-space update, first inverse z pass
   const KPlane P(rp, sh, kx, MODE, is_c, 1.0f / (float)(NY * NZ));

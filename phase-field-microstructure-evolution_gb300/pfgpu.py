@@ -715,17 +715,28 @@ class Pool:
 
     def submit(self, params, phi: np.ndarray, con: np.ndarray, nsteps: int):
         """Queue a run; returns (id, device ordinal)."""
+        return self.submit_aos(params, to_aos(phi), np.ascontiguousarray(con, dtype=np.float64), nsteps)
+
+    def submit_aos(self, params, phi_aos: np.ndarray, con: np.ndarray, nsteps: int):
+        """submit() with the order parameters already in the Fortran
+        phi(var,x,y,z) layout (C-contiguous float64 [z][y][x][var]), which the
+        library copies as they are."""
+        assert phi_aos.dtype == np.float64 and phi_aos.flags.c_contiguous and con.flags.c_contiguous
         cfg = make_config(params, PF_FP32_FUSED, 0)
-        a = to_aos(phi)
-        c = np.ascontiguousarray(con, dtype=np.float64)
         rid, dev = C.c_longlong(), C.c_int()
-        rc = self.lib.pf_pool_submit(self.h, C.byref(cfg), _dp(a), _dp(c), int(nsteps), C.byref(rid), C.byref(dev))
+        rc = self.lib.pf_pool_submit(self.h, C.byref(cfg), _dp(phi_aos), _dp(con), int(nsteps), C.byref(rid),
+                                     C.byref(dev))
         if rc != PF_OK:
             raise PFError(rc, self.lib.pf_pool_last_error().decode())
         self._shape[rid.value] = (params.var, params.Nz, params.Ny, params.Nx)
         return rid.value, dev.value
 
     def wait(self, rid: int, timeout: float = -1.0):
+        a, c, d, t = self.wait_aos(rid, timeout)
+        return from_aos(a), c, d, t
+
+    def wait_aos(self, rid: int, timeout: float = -1.0):
+        """wait() returning the order parameters in the phi(var,x,y,z) layout."""
         var, nz, ny, nx = self._shape.pop(rid)
         a = np.empty((nz, ny, nx, var))
         c = np.empty((nz, ny, nx))
@@ -736,7 +747,7 @@ class Pool:
             self._shape[rid] = (var, nz, ny, nx)
         if rc != PF_OK:
             raise PFError(rc, self.lib.pf_pool_last_error().decode())
-        return from_aos(a), c, d.as_dict(), {k: getattr(t, k) for k, _ in t._fields_}
+        return a, c, d.as_dict(), {k: getattr(t, k) for k, _ in t._fields_}
 
     def close(self):
         if getattr(self, "h", None):
