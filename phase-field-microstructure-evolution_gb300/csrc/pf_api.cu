@@ -119,7 +119,6 @@ static int build_tables(int Nx, int Ny, int Nz, DevTables& t) {
   Shape& s = t.sh;
   s.Nx = Nx; s.Ny = Ny; s.Nz = Nz; s.Kx = Kx;
   s.plane0 = 0;
-  s.pref_x = 0;
   s.pref_yz = 0;
   s.twM = (const float2*)(b + off_tw[0]);
   s.twN = (const float2*)(b + off_tw[1]);
@@ -539,17 +538,7 @@ static void apply_variants(pf_batch* b, const XKernels& xk, const YZKernels& yk)
   }
   b->tab.sh.nblk_x = b->Nz * (b->Ny / xk.wy);
   b->tab.sh.nblk_yz = yk.cluster * b->nF * b->Kx;
-  // L2 prefetch distances: the CTAs resident at once
-  b->tab.sh.pref_x = 0;
-  if (xk.pref) {
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)xk.bulk, xk.threads, b->smem_bulk) !=
-        cudaSuccess) {
-      cudaGetLastError();
-      occ = 0;
-    }
-    b->tab.sh.pref_x = occ * b->nsm;
-  }
+  // L2 prefetch distance of the yz variants that prefetch: the CTAs resident at once
   b->tab.sh.pref_yz = yk.pref ? yz_clusters(b, yk) * yk.cluster : 0;
   apply_xj(b, xk);
 }
@@ -622,6 +611,16 @@ static int tune_batch(pf_batch* b) {
         }
       for (int i : ys)
         if (ty[i] < ty[by]) by = i;
+      if (env_int("PFGPU_AUTOTUNE_REPORT", 0)) {  // every variant's best time per step, on stderr
+        for (int i : xs)
+          fprintf(stderr, "pfgpu autotune %s x %d wy=%d threads=%d%s%s: %.4f ms/step%s\n", key, i, xv[i].wy,
+                  xv[i].threads, xv[i].cl ? ",cluster=2" : (xv[i].tma ? ",tma" : ""), xv[i].tag, tx[i] / REPS,
+                  i == bx ? " (chosen)" : "");
+        for (int i : ys)
+          fprintf(stderr, "pfgpu autotune %s yz %d cluster=%d threads=%d%s%s: %.4f ms/step%s\n", key, i,
+                  yv[i].cluster, yv[i].threads, yv[i].inpl ? ",in-place" : "", yv[i].pref ? ",L2-prefetch" : "",
+                  ty[i] / REPS, i == by ? " (chosen)" : "");
+      }
       // the xj pass (variable mobility) alone, over every variant that fits one field
       apply_variants(b, xv[bx], yv[by]);
       bj = bx;

@@ -19,7 +19,6 @@ struct XKernels {
   int tma = 0;  // > 0: the bulk kernel is the persistent TMA-staged x_pass_tma_kernel, at most this many CTAs per SM
   size_t (*bulk_smem)(int nF) = nullptr;  // its dynamic shared memory (cluster and TMA variants)
   const char* tag = "";  // how the tile is loaded and walked, for reports
-  int pref = 0;          // 1: the bulk kernel prefetches the next generation's tiles into L2 (Shape::pref_x)
 };
 
 // ... and of the yz pass (all three modes).

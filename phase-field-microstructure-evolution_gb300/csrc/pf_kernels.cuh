@@ -86,10 +86,10 @@ struct Shape {
   int nblk_x;   // blocks of the x pass per run
   int nblk_yz;  // blocks of the yz pass per run
   int plane0;   // first (field, kx) plane of a yz-pass launch (a launch may cover a subset)
-  // L2 prefetch distance in CTAs of the x / yz pass variants that prefetch:
-  // the CTAs resident at once, so that CTA b fetches into L2 what CTA b + pref
-  // (which starts about when b ends) will read; 0: none
-  int pref_x, pref_yz;
+  // L2 prefetch distance in CTAs of the yz variants that prefetch: the CTAs
+  // resident at once, so that CTA b fetches into L2 what CTA b + pref (which
+  // starts about when b ends) will read; 0: none
+  int pref_yz;
 };
 
 // ---------------------------------------------------------------------------
@@ -248,6 +248,17 @@ __device__ __forceinline__ float2 ld_spec(const float2* src, size_t stride, int 
   if constexpr (SRC == SPEC_INPLACE) return src[x_spec_slot<M>(kx)];
   else if constexpr (SRC == SPEC_SMEM) return src[(size_t)kx * stride];
   else return __ldg(src + (size_t)kx * stride);
+}
+
+// Run pair of item group q of a line (x_inv_runs / x_fwd_runs), q < N2/2 + 1:
+// the pairs (pr, N2 - pr), 0 < pr < N2/2, first, then the single runs 0 and
+// (N2 even) N2/2.  A pair item costs two DFT_N1, a single one, so with the
+// pairs handed out first the last round of items holds only single runs
+// (132 lines at N2 = 8 and 512 threads: 3 rounds of DFT_N1 instead of 4).
+template <int M>
+__device__ __forceinline__ int x_run_pair(int q) {
+  constexpr int N2 = Line<M>::N2, NPR = (N2 - 1) / 2;
+  return q < NPR ? q + 1 : (q == NPR ? 0 : N2 / 2);
 }
 
 // Inverse x transform, first half: read the half spectrum of line (f, yy)
@@ -596,18 +607,18 @@ __device__ __forceinline__ void bulk_tile(float2* smem, const RunParams& rp, con
       if (rp.mobility != MOB_CONST)
         *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = mob;
     }
-    return;
-  }
-  for (int it = threadIdx.x; it < WY * PM; it += T) {
-    const int yy = it / PM, ps = it - yy * PM;
-    const int q = ps / (N1 + 1), r = ps - q * (N1 + 1);
-    if (r == N1 || ps >= LM::RAW) continue;  // pad slot
-    const int m = q * N1 + r;
-    float2 dfdc, mob;
-    bulk_slot<PM, WY>(smem, yy, ps, rp, dfdc, mob, acc);
-    smem[(rp.V * WY + yy) * PM + ps] = dfdc;
-    if (rp.mobility != MOB_CONST)
-      *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = mob;
+  } else {
+    for (int it = threadIdx.x; it < WY * PM; it += T) {
+      const int yy = it / PM, ps = it - yy * PM;
+      const int q = ps / (N1 + 1), r = ps - q * (N1 + 1);
+      if (r == N1 || ps >= LM::RAW) continue;  // pad slot
+      const int m = q * N1 + r;
+      float2 dfdc, mob;
+      bulk_slot<PM, WY>(smem, yy, ps, rp, dfdc, mob, acc);
+      smem[(rp.V * WY + yy) * PM + ps] = dfdc;
+      if (rp.mobility != MOB_CONST)
+        *reinterpret_cast<float2*>(rp.mob + ((size_t)z * sh.Ny + y0 + yy) * NX + 2 * m) = mob;
+    }
   }
 }
 
@@ -687,11 +698,8 @@ __device__ __forceinline__ void prefetch_l2_warp(const void* p, size_t bytes, in
 // ASYNC: the tile's half spectra are copied into the line buffer by cp.async
 // (all of them in flight at once, no registers held) in the in-place slot
 // order, and the inverse transform then runs in place; otherwise each item
-// loads its own inputs from global memory.  PREF (with ASYNC, bulk mode): once
-// its own spectra have arrived, the CTA prefetches into L2 the spectra of tile
-// blockIdx.x + sh.pref_x, which starts about when this one ends, so that the
-// HBM reads of the next generation of CTAs overlap this one's arithmetic.
-template <int NX, int WY, int T, int MODE, bool PHYS = true, bool ASYNC = false, bool PREF = false>
+// loads its own inputs from global memory.
+template <int NX, int WY, int T, int MODE, bool PHYS = true, bool ASYNC = false>
 __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   constexpr int M = NX / 2;
   using LM = Line<M>;
@@ -732,24 +740,13 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
       }
       cp_async_wait_all();
       __syncthreads();
-      if constexpr (PREF && MODE == MODE_BULK) {
-        const int t2 = (int)blockIdx.x + sh.pref_x;
-        if (sh.pref_x > 0 && t2 < (int)gridDim.x) {
-          const int z2 = t2 / ny_tiles;
-          const size_t row2 = (size_t)z2 * sh.Ny + (size_t)(t2 - z2 * ny_tiles) * WY;
-          for (int it = threadIdx.x; it < nF * KX; it += T) {
-            const int kx = it % KX, f = it / KX;
-            prefetch_l2(src + f * fstride + (size_t)kx * plane + row2, WY * 8);
-          }
-        }
-      }
       for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
-        const int l = it % (nF * WY), pr = it / (nF * WY);
+        const int l = it % (nF * WY), pr = x_run_pair<M>(it / (nF * WY));
         x_inv_runs<M, SPEC_INPLACE>(smem + l * PM, 0, smem + l * PM, pr, sh.twN);
       }
     } else {
       for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
-        const int l = it % (nF * WY), pr = it / (nF * WY);
+        const int l = it % (nF * WY), pr = x_run_pair<M>(it / (nF * WY));
         const int f = l / WY, yy = l - f * WY;
         x_inv_runs<M>(src + f * fstride + row_off + yy, plane, smem + l * PM, pr, sh.twN);
       }
@@ -794,7 +791,7 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
   float2* __restrict__ dst = (MODE == MODE_BULK) ? rp.D : (MODE == MODE_XJ ? rp.J : rp.Sm);
   const float scale = 1.0f / (float)NX;
   for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
-    const int l = it % (nF * WY), pr = it / (nF * WY);
+    const int l = it % (nF * WY), pr = x_run_pair<M>(it / (nF * WY));
     const int f = l / WY, yy = l - f * WY;
     x_fwd_runs<M>(dst + f * fstride + row_off + yy, plane, smem + l * PM, pr, scale, sh.twN);
   }
@@ -870,7 +867,7 @@ __global__ void __launch_bounds__(T, MINB) x_pass_tma_kernel(const RunParams* __
     parity ^= 1u;
     // 1. inverse x transform from the staged half spectra (element kx of row yy at [kx][yy])
     for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
-      const int l = it % (nF * WY), pr = it / (nF * WY);
+      const int l = it % (nF * WY), pr = x_run_pair<M>(it / (nF * WY));
       const int f = l / WY, yy = l - f * WY;
       x_inv_runs<M, SPEC_SMEM>(stage + (size_t)f * G::FSTRIDE + yy, WY, smem + l * PM, pr, sh.twN);
     }
@@ -888,7 +885,7 @@ __global__ void __launch_bounds__(T, MINB) x_pass_tma_kernel(const RunParams* __
     __syncthreads();
     const float scale = 1.0f / (float)NX;
     for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
-      const int l = it % (nF * WY), pr = it / (nF * WY);
+      const int l = it % (nF * WY), pr = x_run_pair<M>(it / (nF * WY));
       const int f = l / WY, yy = l - f * WY;
       x_fwd_runs<M>(rp.D + f * fstride + row_off + yy, plane, smem + l * PM, pr, scale, sh.twN);
     }
@@ -1559,10 +1556,7 @@ __device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
   }
 }
 
-// PREF (main mode): before its k-space update the CTA prefetches into L2 the
-// D~ and k-space planes of CTA blockIdx.x + sh.pref_yz (about one generation
-// of resident CTAs later).
-template <int NY, int NZ, int T, int MODE, bool RAWP = false, bool PREF = false>
+template <int NY, int NZ, int T, int MODE, bool RAWP = false>
 __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using LY = Line<NY>;
   using LZ = Line<NZ>;
@@ -1614,14 +1608,6 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   __syncthreads();
   colA<NY, NZ, T, false, RAWP>(U, sh.twZ);
   __syncthreads();
-  if constexpr (PREF && MODE == YZ_MAIN) {
-    const int p2 = p + sh.pref_yz;
-    if (sh.pref_yz > 0 && (int)blockIdx.x + sh.pref_yz < (int)gridDim.x && threadIdx.x < 64) {
-      const size_t poff2 = (size_t)p2 * plane_elems;  // (f2 Kx + kx2) planes
-      prefetch_l2_warp((threadIdx.x < 32 ? rp.D : rp.Sk) + poff2, plane_elems * 8, threadIdx.x & 31);
-    }
-  }
-
   // 2. last forward z pass, pointwise k-space update, first inverse z pass
   const KPlane P(rp, sh, kx, MODE, is_c, 1.0f / (float)(NY * NZ));
   const float wkx = (kx == 0 || 2 * kx == sh.Nx) ? 1.0f : 2.0f;
@@ -1812,7 +1798,7 @@ __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restric
 
   // 1. inverse x transform of the local fields
   for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
-    const int l = it % (nloc * WY), pr = it / (nloc * WY);
+    const int l = it % (nloc * WY), pr = x_run_pair<M>(it / (nloc * WY));
     const int fl = l / WY, yy = l - fl * WY;
     x_inv_runs<M>(rp.Sm + (fbase + fl) * fstride + row_off + yy, plane, lines + l * PM, pr, sh.twN);
   }
@@ -1943,7 +1929,7 @@ __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restric
   __syncthreads();
   const float scale = 1.0f / (float)NX;
   for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
-    const int l = it % (nloc * WY), pr = it / (nloc * WY);
+    const int l = it % (nloc * WY), pr = x_run_pair<M>(it / (nloc * WY));
     const int fl = l / WY, yy = l - fl * WY;
     x_fwd_runs<M>(rp.D + (fbase + fl) * fstride + row_off + yy, plane, lines + l * PM, pr, scale, sh.twN);
   }

@@ -46,13 +46,12 @@ static int addtma(XKernels* out, int n) {
 }
 
 // every mode with the tile's spectra copied in by cp.async and transformed in
-// place (PHYS: the bulk walk over physical slots; PREF: the bulk kernel
-// prefetches the next generation's tiles into L2)
-template <int NX, int WY, int T, bool PHYS = false, bool PREF = false>
+// place (PHYS: the bulk walk over physical slots)
+template <int NX, int WY, int T, bool PHYS = false>
 static int addas(XKernels* out, int n) {
   if (n >= kMaxVariants) return n;
   XKernels& k = out[n];
-  k.bulk = x_pass_kernel<NX, WY, T, MODE_BULK, PHYS, true, PREF>;
+  k.bulk = x_pass_kernel<NX, WY, T, MODE_BULK, PHYS, true>;
   k.xj = x_pass_kernel<NX, WY, T, MODE_XJ, PHYS, true>;
   k.imp = x_pass_kernel<NX, WY, T, MODE_IMPORT>;
   k.exp = x_pass_kernel<NX, WY, T, MODE_EXPORT, PHYS, true>;
@@ -61,8 +60,7 @@ static int addas(XKernels* out, int n) {
   k.cl = 0;
   k.tma = 0;
   k.bulk_smem = nullptr;
-  k.tag = PREF ? (PHYS ? ",async,L2-prefetch" : ",async,logical,L2-prefetch") : (PHYS ? ",async" : ",async,logical");
-  k.pref = PREF ? 1 : 0;
+  k.tag = PHYS ? ",async" : ",async,logical";
   return n + 1;
 }
 
@@ -115,7 +113,6 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = addas<128, 8, 256>(out, n); n = addas<128, 8, 256, true>(out, n); n = addas<128, 4, 256>(out, n);
       // many rows for the one-field xj pass (its bulk mode does not fit: never chosen for the bulk pass)
       n = add<128, 32, 256>(out, n);
-      n = addas<128, 8, 256, false, true>(out, n);
       break;
     case 256:
       n = add<256, 4, 256>(out, n); n = add<256, 2, 256>(out, n); n = add<256, 4, 512>(out, n);
@@ -123,7 +120,6 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = addtma<256, 4, 512>(out, n); n = addtma<256, 2, 512>(out, n);
       n = addas<256, 4, 512>(out, n); n = addas<256, 2, 256>(out, n);
       n = addcl<256, 8, 512>(out, n);  // fields split over two CTAs: 8-row (64-byte) tiles at 33 fields
-      n = addas<256, 4, 512, false, true>(out, n);
       break;
     default: break;
   }
