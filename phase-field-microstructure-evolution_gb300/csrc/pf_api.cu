@@ -133,16 +133,16 @@ static int build_tables(int Nx, int Ny, int Nz, DevTables& t) {
 static size_t x_smem(int nx, int nF, int wy) {
   int pitch;
   switch (nx) {
-    case 16: pitch = Line<8>::PITCH; break;
-    case 32: pitch = Line<16>::PITCH; break;
-    case 64: pitch = Line<32>::PITCH; break;
-    case 96: pitch = Line<48>::PITCH; break;
-    case 128: pitch = Line<64>::PITCH; break;
-    case 256: pitch = Line<128>::PITCH; break;
-    case 80: pitch = Line<40>::PITCH; break;
-    case 160: pitch = Line<80>::PITCH; break;
-    case 200: pitch = Line<100>::PITCH; break;
-    case 102: pitch = Line<51>::PITCH; break;
+    case 16: pitch = XLine<8>::PITCH; break;
+    case 32: pitch = XLine<16>::PITCH; break;
+    case 64: pitch = XLine<32>::PITCH; break;
+    case 96: pitch = XLine<48>::PITCH; break;
+    case 128: pitch = XLine<64>::PITCH; break;
+    case 256: pitch = XLine<128>::PITCH; break;
+    case 80: pitch = XLine<40>::PITCH; break;
+    case 160: pitch = XLine<80>::PITCH; break;
+    case 200: pitch = XLine<100>::PITCH; break;
+    case 102: pitch = XLine<51>::PITCH; break;
     default: return 0;
   }
   return (size_t)nF * wy * pitch * sizeof(float2);
@@ -495,7 +495,8 @@ static void describe_variants(pf_batch* b) {
   char buf[256];
   snprintf(buf, sizeof buf, "x:wy=%d,threads=%d%s%s yz:cluster=%d,threads=%d%s%s xj:wy=%d,threads=%d%s", b->xk.wy,
            b->xk.threads, b->xk.cl ? ",cluster=2" : (b->xk.tma ? ",tma" : ""), b->xk.tag, b->yk.cluster,
-           b->yk.threads, b->yk.inpl ? ",in-place" : "", b->yk.pref ? ",L2-prefetch" : "", b->xjk.wy,
+           b->yk.threads, b->yk.inpl ? ",in-place" : "",
+           b->yk.pref ? (b->yk.stg ? ",L2-prefetch,staged" : ",L2-prefetch") : (b->yk.stg ? ",staged" : ""), b->xjk.wy,
            b->xjk.threads, b->xjk.tag);
   b->variant = buf;
 }
@@ -618,7 +619,8 @@ static int tune_batch(pf_batch* b) {
                   i == bx ? " (chosen)" : "");
         for (int i : ys)
           fprintf(stderr, "pfgpu autotune %s yz %d cluster=%d threads=%d%s%s: %.4f ms/step%s\n", key, i,
-                  yv[i].cluster, yv[i].threads, yv[i].inpl ? ",in-place" : "", yv[i].pref ? ",L2-prefetch" : "",
+                  yv[i].cluster, yv[i].threads, yv[i].inpl ? ",in-place" : "",
+                  yv[i].pref ? (yv[i].stg ? ",L2-prefetch,staged" : ",L2-prefetch") : (yv[i].stg ? ",staged" : ""),
                   ty[i] / REPS, i == by ? " (chosen)" : "");
       }
       // the xj pass (variable mobility) alone, over every variant that fits one field

@@ -351,10 +351,12 @@ template <> struct Plan<192> { static constexpr int N1 = 16, N2 = 12; };
 template <> struct Plan<200> { static constexpr int N1 = 20, N2 = 10; };
 template <> struct Plan<256> { static constexpr int N1 = 16, N2 = 16; };
 
-template <int L>
+// Line<L>: the plan's factorization; Line<L, A, B> any other L = A * B.
+template <int L, int A = Plan<L>::N1, int B = Plan<L>::N2>
 struct Line {
-  static constexpr int N1 = Plan<L>::N1;
-  static constexpr int N2 = Plan<L>::N2;
+  static constexpr int LEN = L;
+  static constexpr int N1 = A;
+  static constexpr int N2 = B;
   static_assert(N1 * N2 == L, "bad plan");
   // padded storage: one pad slot after every run of N1, odd line pitch
   static constexpr int RAW = N2 * (N1 + 1);

@@ -29,6 +29,7 @@ struct YZKernels {
   size_t smem;   // dynamic shared memory per CTA
   int inpl = 0;  // 1: the cluster exchanges the plane in place (one buffer per CTA)
   int pref = 0;  // 1: the main kernel prefetches the next generation's planes into L2 (Shape::pref_yz)
+  int stg = 0;   // 1: the update's k-space values are staged in shared memory by cp.async
 };
 
 // Variant lists: each translation unit appends the variants it compiled for a
@@ -72,7 +73,7 @@ inline bool get_yz_kernels(int ny, int nz, YZKernels* out) {
 // x-pass shared memory for nF fields
 template <int NX>
 constexpr size_t x_smem_bytes(int nF, int wy) {
-  return (size_t)nF * wy * Line<NX / 2>::PITCH * sizeof(float2);
+  return (size_t)nF * wy * XLine<NX / 2>::PITCH * sizeof(float2);
 }
 
 void set_error(const std::string& msg);

@@ -197,12 +197,28 @@ __device__ __forceinline__ void post_pair(float2 zk, float2 zm, float2 wk, float
   xm = __fmul2_rn(__ffma2_rn(s, make_float2(1.f, -1.f), mie2), hh);
 }
 
+// Factorization of the x pass's lines (M = Nx/2 complex points): the plan's,
+// except M = 128 as 8 x 16.  The x pass holds a tile of every field in one CTA
+// (one CTA per SM at Nx = 256), so its warps per SM are set by the registers
+// per thread: with runs of 8 the largest per-thread state of its passes is one
+// DFT_16 instead of a pair of DFT_16, which lets a CTA of 768 threads fit.
+template <int M>
+struct XPlan {
+  static constexpr int N1 = Plan<M>::N1, N2 = Plan<M>::N2;
+};
+template <>
+struct XPlan<128> {
+  static constexpr int N1 = 8, N2 = 16;
+};
+template <int M>
+using XLine = Line<M, XPlan<M>::N1, XPlan<M>::N2>;
+
 // pass A over a runtime number of lines (pitch P, T threads).  A warp takes 32
 // consecutive lines at one column n1: with an odd pitch those 32 accesses hit
 // distinct bank pairs.
 template <int L, int P, int T, bool INV>
 __device__ __forceinline__ void passA_rt(float2* buf, int NL, const float2* __restrict__ tw) {
-  constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
+  constexpr int N1 = XLine<L>::N1, N2 = XLine<L>::N2;
   const int nlb = (NL + 31) >> 5;  // groups of 32 lines
   const int items = nlb * 32 * N1;
   for (int it = threadIdx.x; it < items; it += T) {
@@ -239,7 +255,7 @@ enum SpecSrc { SPEC_GLOBAL = 0, SPEC_SMEM = 1, SPEC_INPLACE = 2 };
 
 template <int M>
 __device__ __forceinline__ int x_spec_slot(int kx) {
-  constexpr int N1 = Line<M>::N1, N2 = Line<M>::N2;
+  constexpr int N1 = XLine<M>::N1, N2 = XLine<M>::N2;
   return kx == M ? N1 : (N1 + 1) * (kx % N2) + kx / N2;
 }
 
@@ -257,7 +273,7 @@ __device__ __forceinline__ float2 ld_spec(const float2* src, size_t stride, int 
 // (132 lines at N2 = 8 and 512 threads: 3 rounds of DFT_N1 instead of 4).
 template <int M>
 __device__ __forceinline__ int x_run_pair(int q) {
-  constexpr int N2 = Line<M>::N2, NPR = (N2 - 1) / 2;
+  constexpr int N2 = XLine<M>::N2, NPR = (N2 - 1) / 2;
   return q < NPR ? q + 1 : (q == NPR ? 0 : N2 / 2);
 }
 
@@ -267,7 +283,7 @@ __device__ __forceinline__ int x_run_pair(int q) {
 template <int M, int SRC = SPEC_GLOBAL>
 __device__ __forceinline__ void x_inv_runs(const float2* src, size_t plane, float2* line, int pr,
                                            const float2* __restrict__ twN) {  // src may be line (in place)
-  constexpr int N1 = Line<M>::N1, N2 = Line<M>::N2;
+  constexpr int N1 = XLine<M>::N1, N2 = XLine<M>::N2;
   if (pr > 0 && 2 * pr < N2) {
     const int ra = pr, rb = N2 - pr;
     float2 a[N1], b[N1];
@@ -329,7 +345,7 @@ __device__ __forceinline__ void x_inv_runs(const float2* src, size_t plane, floa
 template <int M>
 __device__ __forceinline__ void x_fwd_runs(float2* __restrict__ dst, size_t plane, const float2* line, int pr,
                                            float scale, const float2* __restrict__ twN) {
-  constexpr int N1 = Line<M>::N1, N2 = Line<M>::N2;
+  constexpr int N1 = XLine<M>::N1, N2 = XLine<M>::N2;
   const float h = 0.5f * scale;
   if (pr > 0 && 2 * pr < N2) {
     const int ra = pr, rb = N2 - pr;
@@ -410,6 +426,7 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
   // pass 1: S2 = sum phi^2, Smat = sum_{i<V-1} phi^2, S4, N4, f_eta pair
   // sum, both cells of the slot at once in packed FP32 pairs
   float2 pre = make_float2(0.f, 0.f), n4v = make_float2(0.f, 0.f), prs = make_float2(0.f, 0.f);
+#pragma unroll 4
   for (int f = 0; f < V - 1; ++f) {
     const float2 p = base[f * FS];
     const float2 a = __fmul2_rn(p, p);
@@ -508,6 +525,7 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
     const float2 cterm = make_float2(fmaf(2.f, gP[0], -1.f), fmaf(2.f, gP[1], -1.f));
     const float2 sm = make_float2(Smat[0], Smat[1]);
     float2 ds = make_float2(0.f, 0.f);
+#pragma unroll 4
     for (int f = 0; f < V - 1; ++f) {
       const float2 p = base[f * FS];
       const float2 p2 = __fmul2_rn(p, p);
@@ -595,7 +613,7 @@ template <int NX, int WY, int T, bool PHYS = true>
 __device__ __forceinline__ void bulk_tile(float2* smem, const RunParams& rp, const Shape& sh, int z, int y0,
                                           BulkAcc& acc) {
   constexpr int M = NX / 2;
-  using LM = Line<M>;
+  using LM = XLine<M>;
   constexpr int PM = LM::PITCH, N1 = LM::N1;
   if constexpr (!PHYS) {  // walk over the logical cells (a half warp spans N1 + 1 slots per N1 cells)
     for (int it = threadIdx.x; it < WY * M; it += T) {
@@ -682,6 +700,13 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // Prefetch [p, p + bytes) into L2 (cp.async.bulk.prefetch): no registers, no
 // completion to wait for.  p 16-byte aligned, bytes a multiple of 16.
 __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
@@ -702,7 +727,7 @@ __device__ __forceinline__ void prefetch_l2_warp(const void* p, size_t bytes, in
 template <int NX, int WY, int T, int MODE, bool PHYS = true, bool ASYNC = false>
 __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   constexpr int M = NX / 2;
-  using LM = Line<M>;
+  using LM = XLine<M>;
   constexpr int PM = LM::PITCH;
   constexpr int NP = LM::N2 / 2 + 1;  // run pairs per line
   // run pairs (pr, N2 - pr) for 0 < pr < N2/2, run 0 alone, and for even N2
@@ -820,7 +845,7 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
 // ---------------------------------------------------------------------------
 template <int NX, int WY>
 struct XTMA {
-  static constexpr int M = NX / 2, KX = M + 1, PM = Line<M>::PITCH;
+  static constexpr int M = NX / 2, KX = M + 1, PM = XLine<M>::PITCH;
   // staging of one field, a multiple of 128 bytes so that every TMA
   // destination starts on a 128-byte boundary
   static constexpr int FSTRIDE = ((KX * WY * 8 + 127) / 128) * 16;  // float2 elements
@@ -832,7 +857,7 @@ template <int NX, int WY, int T, int MINB = 1>
 __global__ void __launch_bounds__(T, MINB) x_pass_tma_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = XTMA<NX, WY>;
   constexpr int M = G::M, KX = G::KX, PM = G::PM;
-  using LM = Line<M>;
+  using LM = XLine<M>;
   constexpr int NP = LM::N2 / 2 + 1;
   extern __shared__ __align__(128) unsigned char xsm[];
   const RunParams& rp = runs[blockIdx.y];
@@ -1337,7 +1362,9 @@ __device__ __forceinline__ void passB(float2* buf) {
 // PREF (main mode): before its k-space update the CTA prefetches into L2 the
 // D~ rows and k-space block that CTA blockIdx.x + sh.pref_yz (a multiple of C:
 // the same cluster rank, about one generation of resident CTAs later) reads.
-template <int NY, int NZ, int C, int T, int MODE, bool INPL = false, bool PREF = false>
+// STG: as in yz1_kernel, the k-space values of each round of update items are
+// staged by cp.async behind the plane buffer.
+template <int NY, int NZ, int C, int T, int MODE, bool INPL = false, bool PREF = false, bool STG = false>
 __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = YZ<NY, NZ, C>;
   using LY = Line<NY>;
@@ -1361,6 +1388,19 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   const bool is_c = (f == rp.V);
   const bool var_c = (MODE == YZ_MAIN) && is_c && rp.mobility != MOB_CONST;
   const int z0 = r * G::LA;
+  constexpr bool STAGED = STG && MODE != YZ_IMPORT;
+  constexpr size_t SK1 = (size_t)NY * N2z;  // stride of k1 in the k-space plane
+  float2* stage = smem + (INPL ? (G::UA > G::UB ? G::UA : G::UB) : G::UA + G::UB);  // [k1][item of the round]
+  // copy the k-space values of update round j of this CTA into the stage
+  auto stage_round = [&](int j) {
+    static_assert(!STAGED || ((G::LB * N2z) % T == 0 && T % 2 == 0), "whole rounds of pairs");
+    for (int u2 = threadIdx.x; u2 < N1z * T / 2; u2 += T) {
+      const int e = 2 * u2, k1 = e / T, off = e - k1 * T;
+      cp_async16(stage + e, rp.Sk + poff + k1 * SK1 + (size_t)r * G::LB * N2z + (size_t)j * T + off);
+    }
+    cp_async_commit();
+  };
+  if constexpr (STAGED) stage_round(0);
 
   // 1. forward y transform of the mixed-space input rows z0..z0+LA
   //    (MAIN/IMPORT: D~ or S~; C2: J~'), first pass straight from global
@@ -1429,12 +1469,21 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
       // k-space state of this plane in [k1][y position][k2] order: for every
       // k1 a warp reads and writes consecutive (y position, k2) (coalesced)
       float2* gk = rp.Sk + poff + (size_t)ypos * N2z + k2;
-      constexpr size_t SK1 = (size_t)NY * N2z;  // stride of k1
       float2 d[N1z], u[N1z];
+      if constexpr (STAGED) {
+        cp_async_wait0();
+        __syncthreads();  // round j in the stage for every thread
+#pragma unroll
+        for (int k1 = 0; k1 < N1z; ++k1) u[k1] = stage[k1 * T + threadIdx.x];
+        if (j + 1 < ITER) {
+          __syncthreads();  // every thread has read round j
+          stage_round(j + 1);
+        }
+      }
 #pragma unroll
       for (int k1 = 0; k1 < N1z; ++k1) d[k1] = pb[k1];
       Dft<N1z>::fwd(d);
-      if (MODE != YZ_IMPORT) {
+      if (!STAGED && MODE != YZ_IMPORT) {
 #pragma unroll
         for (int k1 = 0; k1 < N1z; ++k1) u[k1] = gk[k1 * SK1];
       }
@@ -1525,6 +1574,11 @@ template <int NY, int NZ, bool RAWP = false>
 struct YZ1 {
   static constexpr int PY = RAWP ? Line<NY>::RAW : Line<NY>::PITCH;
   static constexpr size_t SMEM = (size_t)NZ * PY * sizeof(float2);
+  // with a k-space stage for one round of T update items (N1z values each)
+  template <int T>
+  static constexpr size_t smem_staged() {
+    return SMEM + (size_t)Line<NZ>::N1 * T * sizeof(float2);
+  }
 };
 
 // column pass A (forward or inverse) over the NY y positions
@@ -1556,7 +1610,11 @@ __device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
   }
 }
 
-template <int NY, int NZ, int T, int MODE, bool RAWP = false>
+// STG: the k-space values of each round of T update items are copied by
+// cp.async into a stage behind the plane (the first round's at the start of
+// the kernel, the next round's while the current one is updated), so that the
+// update reads them from shared memory instead of waiting on global loads.
+template <int NY, int NZ, int T, int MODE, bool RAWP = false, bool STG = false>
 __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using LY = Line<NY>;
   using LZ = Line<NZ>;
@@ -1575,6 +1633,19 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   const size_t poff = ((size_t)f * Kx + kx) * plane_elems;
   const bool is_c = (f == rp.V);
   const bool var_c = (MODE == YZ_MAIN) && is_c && rp.mobility != MOB_CONST;
+  constexpr bool STAGED = STG && MODE != YZ_IMPORT;
+  constexpr size_t SK1 = (size_t)N2z * NY;  // stride of k1 in the k-space plane
+  float2* stage = U + NZ * PY;              // [k1][item of the round] (STAGED)
+  // copy the k-space values of update round j (items j T .. j T + T - 1) into the stage
+  auto stage_round = [&](int j) {
+    static_assert(!STAGED || ((NY * N2z) % T == 0 && T % 2 == 0), "whole rounds of pairs");
+    for (int u2 = threadIdx.x; u2 < N1z * T / 2; u2 += T) {
+      const int e = 2 * u2, k1 = e / T, off = e - k1 * T;
+      cp_async16(stage + e, rp.Sk + poff + k1 * SK1 + (size_t)j * T + off);
+    }
+    cp_async_commit();
+  };
+  if constexpr (STAGED) stage_round(0);
 
   // 1. forward y transform of all NZ rows, first pass straight from global
   {
@@ -1624,9 +1695,17 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
       // k-space state of this plane in [k1][k2][y position] order: for every
       // k1 a warp reads and writes 32 consecutive y positions (coalesced)
       float2* gk = rp.Sk + poff + it;  // it == k2 NY + yp
-      constexpr size_t SK1 = (size_t)N2z * NY;  // stride of k1
       float2 d[N1z], u[N1z];
-      if (MODE != YZ_IMPORT) {
+      if constexpr (STAGED) {
+        cp_async_wait0();
+        __syncthreads();  // round j in the stage for every thread
+#pragma unroll
+        for (int k1 = 0; k1 < N1z; ++k1) u[k1] = stage[k1 * T + threadIdx.x];
+        if (j + 1 < ITER) {
+          __syncthreads();  // every thread has read round j
+          stage_round(j + 1);
+        }
+      } else if (MODE != YZ_IMPORT) {
 #pragma unroll
         for (int k1 = 0; k1 < N1z; ++k1) u[k1] = gk[k1 * SK1];
       }
@@ -1713,7 +1792,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
 template <int NX, int WY>
 struct XCL {
   static constexpr int M = NX / 2;
-  static constexpr int PM = Line<M>::PITCH;
+  static constexpr int PM = XLine<M>::PITCH;
   static constexpr int S = WY * M;  // float2 slots (two cells each) per CTA
   static constexpr int NA = 7;      // per-slot arrays: pre, n4, pairs, mabs (partials), nn (partial), phiP, c
   static constexpr size_t smem(int nF) { return ((size_t)((nF + 1) / 2) * WY * PM + (size_t)NA * S) * sizeof(float2); }
@@ -1773,11 +1852,13 @@ __device__ __forceinline__ CellOut cell_terms(float pp, float c, float pre, floa
   return o;
 }
 
-template <int NX, int WY, int T>
+// ASYNC: the local fields' half spectra arrive by cp.async in the in-place
+// slot order (as in x_pass_kernel), and the inverse transform runs in place.
+template <int NX, int WY, int T, bool ASYNC = false>
 __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = XCL<NX, WY>;
   constexpr int M = G::M, PM = G::PM, S = G::S;
-  using LM = Line<M>;
+  using LM = XLine<M>;
   constexpr int NP = LM::N2 / 2 + 1;
   enum { A_PRE = 0, A_N4, A_PAIRS, A_MABS, A_NN, A_PP, A_C };
   extern __shared__ float2 smem[];
@@ -1797,10 +1878,25 @@ __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restric
   const uint32_t peer_lines = map_rank(smem_addr(lines), peer);
 
   // 1. inverse x transform of the local fields
-  for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
-    const int l = it % (nloc * WY), pr = x_run_pair<M>(it / (nloc * WY));
-    const int fl = l / WY, yy = l - fl * WY;
-    x_inv_runs<M>(rp.Sm + (fbase + fl) * fstride + row_off + yy, plane, lines + l * PM, pr, sh.twN);
+  if constexpr (ASYNC) {
+    constexpr int KX = M + 1;
+    for (int it = threadIdx.x; it < nloc * KX * WY; it += T) {
+      const int yy = it % WY, r = it / WY, kx = r % KX, fl = r / KX;
+      cp_async8(lines + (fl * WY + yy) * PM + x_spec_slot<M>(kx),
+                rp.Sm + (fbase + fl) * fstride + (size_t)kx * plane + row_off + yy);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
+      const int l = it % (nloc * WY), pr = x_run_pair<M>(it / (nloc * WY));
+      x_inv_runs<M, SPEC_INPLACE>(lines + l * PM, 0, lines + l * PM, pr, sh.twN);
+    }
+  } else {
+    for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
+      const int l = it % (nloc * WY), pr = x_run_pair<M>(it / (nloc * WY));
+      const int fl = l / WY, yy = l - fl * WY;
+      x_inv_runs<M>(rp.Sm + (fbase + fl) * fstride + row_off + yy, plane, lines + l * PM, pr, sh.twN);
+    }
   }
   __syncthreads();
   passA_rt<M, PM, T, true>(lines, nloc * WY, sh.twM);

@@ -39,8 +39,8 @@ def test_supported_shapes(lib):
     assert lib.pf_supported_shape(128, 128, 128, 99, 32) == 0  # x-pass rows no longer fit
     assert lib.pf_supported_shape(96, 96, 96, 131, 32) == 1
     assert lib.pf_supported_shape(96, 96, 96, 132, 32) == 0
-    assert lib.pf_supported_shape(256, 256, 256, 105, 32) == 1
-    assert lib.pf_supported_shape(256, 256, 256, 106, 32) == 0
+    assert lib.pf_supported_shape(256, 256, 256, 199, 32) == 1  # one-row tiles of 200 fields
+    assert lib.pf_supported_shape(256, 256, 256, 200, 32) == 0
     assert lib.pf_supported_shape(64, 64, 64, 256, 32) == 0  # var limit
 
 
