@@ -495,8 +495,7 @@ static void describe_variants(pf_batch* b) {
   char buf[256];
   snprintf(buf, sizeof buf, "x:wy=%d,threads=%d%s%s yz:cluster=%d,threads=%d%s%s xj:wy=%d,threads=%d%s", b->xk.wy,
            b->xk.threads, b->xk.cl ? ",cluster=2" : (b->xk.tma ? ",tma" : ""), b->xk.tag, b->yk.cluster,
-           b->yk.threads, b->yk.inpl ? ",in-place" : "",
-           b->yk.pref ? (b->yk.stg ? ",L2-prefetch,staged" : ",L2-prefetch") : (b->yk.stg ? ",staged" : ""), b->xjk.wy,
+           b->yk.threads, b->yk.inpl ? ",in-place" : "", b->yk.pref ? ",L2-prefetch" : "", b->xjk.wy,
            b->xjk.threads, b->xjk.tag);
   b->variant = buf;
 }
@@ -619,8 +618,7 @@ static int tune_batch(pf_batch* b) {
                   i == bx ? " (chosen)" : "");
         for (int i : ys)
           fprintf(stderr, "pfgpu autotune %s yz %d cluster=%d threads=%d%s%s: %.4f ms/step%s\n", key, i,
-                  yv[i].cluster, yv[i].threads, yv[i].inpl ? ",in-place" : "",
-                  yv[i].pref ? (yv[i].stg ? ",L2-prefetch,staged" : ",L2-prefetch") : (yv[i].stg ? ",staged" : ""),
+                  yv[i].cluster, yv[i].threads, yv[i].inpl ? ",in-place" : "", yv[i].pref ? ",L2-prefetch" : "",
                   ty[i] / REPS, i == by ? " (chosen)" : "");
       }
       // the xj pass (variable mobility) alone, over every variant that fits one field

@@ -29,7 +29,6 @@ struct YZKernels {
   size_t smem;   // dynamic shared memory per CTA
   int inpl = 0;  // 1: the cluster exchanges the plane in place (one buffer per CTA)
   int pref = 0;  // 1: the main kernel prefetches the next generation's planes into L2 (Shape::pref_yz)
-  int stg = 0;   // 1: the update's k-space values are staged in shared memory by cp.async
 };
 
 // Variant lists: each translation unit appends the variants it compiled for a

@@ -198,10 +198,9 @@ __device__ __forceinline__ void post_pair(float2 zk, float2 zm, float2 wk, float
 }
 
 // Factorization of the x pass's lines (M = Nx/2 complex points): the plan's,
-// except M = 128 as 8 x 16.  The x pass holds a tile of every field in one CTA
-// (one CTA per SM at Nx = 256), so its warps per SM are set by the registers
-// per thread: with runs of 8 the largest per-thread state of its passes is one
-// DFT_16 instead of a pair of DFT_16, which lets a CTA of 768 threads fit.
+// except M = 128 as 8 x 16.  With runs of 8 the largest per-thread state of
+// the x pass is one DFT_16 instead of a pair of them: 80 registers a thread
+// at Nx = 256 instead of 128 with spills (the same speed at 33 fields).
 template <int M>
 struct XPlan {
   static constexpr int N1 = Plan<M>::N1, N2 = Plan<M>::N2;
@@ -700,13 +699,6 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
 // Prefetch [p, p + bytes) into L2 (cp.async.bulk.prefetch): no registers, no
 // completion to wait for.  p 16-byte aligned, bytes a multiple of 16.
 __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
@@ -1362,9 +1354,7 @@ __device__ __forceinline__ void passB(float2* buf) {
 // PREF (main mode): before its k-space update the CTA prefetches into L2 the
 // D~ rows and k-space block that CTA blockIdx.x + sh.pref_yz (a multiple of C:
 // the same cluster rank, about one generation of resident CTAs later) reads.
-// STG: as in yz1_kernel, the k-space values of each round of update items are
-// staged by cp.async behind the plane buffer.
-template <int NY, int NZ, int C, int T, int MODE, bool INPL = false, bool PREF = false, bool STG = false>
+template <int NY, int NZ, int C, int T, int MODE, bool INPL = false, bool PREF = false>
 __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = YZ<NY, NZ, C>;
   using LY = Line<NY>;
@@ -1388,19 +1378,6 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
   const bool is_c = (f == rp.V);
   const bool var_c = (MODE == YZ_MAIN) && is_c && rp.mobility != MOB_CONST;
   const int z0 = r * G::LA;
-  constexpr bool STAGED = STG && MODE != YZ_IMPORT;
-  constexpr size_t SK1 = (size_t)NY * N2z;  // stride of k1 in the k-space plane
-  float2* stage = smem + (INPL ? (G::UA > G::UB ? G::UA : G::UB) : G::UA + G::UB);  // [k1][item of the round]
-  // copy the k-space values of update round j of this CTA into the stage
-  auto stage_round = [&](int j) {
-    static_assert(!STAGED || ((G::LB * N2z) % T == 0 && T % 2 == 0), "whole rounds of pairs");
-    for (int u2 = threadIdx.x; u2 < N1z * T / 2; u2 += T) {
-      const int e = 2 * u2, k1 = e / T, off = e - k1 * T;
-      cp_async16(stage + e, rp.Sk + poff + k1 * SK1 + (size_t)r * G::LB * N2z + (size_t)j * T + off);
-    }
-    cp_async_commit();
-  };
-  if constexpr (STAGED) stage_round(0);
 
   // 1. forward y transform of the mixed-space input rows z0..z0+LA
   //    (MAIN/IMPORT: D~ or S~; C2: J~'), first pass straight from global
@@ -1469,21 +1446,12 @@ __global__ void __launch_bounds__(T) yz_kernel(const RunParams* __restrict__ run
       // k-space state of this plane in [k1][y position][k2] order: for every
       // k1 a warp reads and writes consecutive (y position, k2) (coalesced)
       float2* gk = rp.Sk + poff + (size_t)ypos * N2z + k2;
+      constexpr size_t SK1 = (size_t)NY * N2z;  // stride of k1
       float2 d[N1z], u[N1z];
-      if constexpr (STAGED) {
-        cp_async_wait0();
-        __syncthreads();  // round j in the stage for every thread
-#pragma unroll
-        for (int k1 = 0; k1 < N1z; ++k1) u[k1] = stage[k1 * T + threadIdx.x];
-        if (j + 1 < ITER) {
-          __syncthreads();  // every thread has read round j
-          stage_round(j + 1);
-        }
-      }
 #pragma unroll
       for (int k1 = 0; k1 < N1z; ++k1) d[k1] = pb[k1];
       Dft<N1z>::fwd(d);
-      if (!STAGED && MODE != YZ_IMPORT) {
+      if (MODE != YZ_IMPORT) {
 #pragma unroll
         for (int k1 = 0; k1 < N1z; ++k1) u[k1] = gk[k1 * SK1];
       }
@@ -1574,11 +1542,6 @@ template <int NY, int NZ, bool RAWP = false>
 struct YZ1 {
   static constexpr int PY = RAWP ? Line<NY>::RAW : Line<NY>::PITCH;
   static constexpr size_t SMEM = (size_t)NZ * PY * sizeof(float2);
-  // with a k-space stage for one round of T update items (N1z values each)
-  template <int T>
-  static constexpr size_t smem_staged() {
-    return SMEM + (size_t)Line<NZ>::N1 * T * sizeof(float2);
-  }
 };
 
 // column pass A (forward or inverse) over the NY y positions
@@ -1610,11 +1573,7 @@ __device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
   }
 }
 
-// STG: the k-space values of each round of T update items are copied by
-// cp.async into a stage behind the plane (the first round's at the start of
-// the kernel, the next round's while the current one is updated), so that the
-// update reads them from shared memory instead of waiting on global loads.
-template <int NY, int NZ, int T, int MODE, bool RAWP = false, bool STG = false>
+template <int NY, int NZ, int T, int MODE, bool RAWP = false>
 __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using LY = Line<NY>;
   using LZ = Line<NZ>;
@@ -1633,19 +1592,6 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   const size_t poff = ((size_t)f * Kx + kx) * plane_elems;
   const bool is_c = (f == rp.V);
   const bool var_c = (MODE == YZ_MAIN) && is_c && rp.mobility != MOB_CONST;
-  constexpr bool STAGED = STG && MODE != YZ_IMPORT;
-  constexpr size_t SK1 = (size_t)N2z * NY;  // stride of k1 in the k-space plane
-  float2* stage = U + NZ * PY;              // [k1][item of the round] (STAGED)
-  // copy the k-space values of update round j (items j T .. j T + T - 1) into the stage
-  auto stage_round = [&](int j) {
-    static_assert(!STAGED || ((NY * N2z) % T == 0 && T % 2 == 0), "whole rounds of pairs");
-    for (int u2 = threadIdx.x; u2 < N1z * T / 2; u2 += T) {
-      const int e = 2 * u2, k1 = e / T, off = e - k1 * T;
-      cp_async16(stage + e, rp.Sk + poff + k1 * SK1 + (size_t)j * T + off);
-    }
-    cp_async_commit();
-  };
-  if constexpr (STAGED) stage_round(0);
 
   // 1. forward y transform of all NZ rows, first pass straight from global
   {
@@ -1695,17 +1641,9 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
       // k-space state of this plane in [k1][k2][y position] order: for every
       // k1 a warp reads and writes 32 consecutive y positions (coalesced)
       float2* gk = rp.Sk + poff + it;  // it == k2 NY + yp
+      constexpr size_t SK1 = (size_t)N2z * NY;  // stride of k1
       float2 d[N1z], u[N1z];
-      if constexpr (STAGED) {
-        cp_async_wait0();
-        __syncthreads();  // round j in the stage for every thread
-#pragma unroll
-        for (int k1 = 0; k1 < N1z; ++k1) u[k1] = stage[k1 * T + threadIdx.x];
-        if (j + 1 < ITER) {
-          __syncthreads();  // every thread has read round j
-          stage_round(j + 1);
-        }
-      } else if (MODE != YZ_IMPORT) {
+      if (MODE != YZ_IMPORT) {
 #pragma unroll
         for (int k1 = 0; k1 < N1z; ++k1) u[k1] = gk[k1 * SK1];
       }
@@ -1852,9 +1790,7 @@ __device__ __forceinline__ CellOut cell_terms(float pp, float c, float pre, floa
   return o;
 }
 
-// ASYNC: the local fields' half spectra arrive by cp.async in the in-place
-// slot order (as in x_pass_kernel), and the inverse transform runs in place.
-template <int NX, int WY, int T, bool ASYNC = false>
+template <int NX, int WY, int T>
 __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restrict__ runs, const Shape sh) {
   using G = XCL<NX, WY>;
   constexpr int M = G::M, PM = G::PM, S = G::S;
@@ -1878,25 +1814,10 @@ __global__ void __launch_bounds__(T) x_pass_cl_kernel(const RunParams* __restric
   const uint32_t peer_lines = map_rank(smem_addr(lines), peer);
 
   // 1. inverse x transform of the local fields
-  if constexpr (ASYNC) {
-    constexpr int KX = M + 1;
-    for (int it = threadIdx.x; it < nloc * KX * WY; it += T) {
-      const int yy = it % WY, r = it / WY, kx = r % KX, fl = r / KX;
-      cp_async8(lines + (fl * WY + yy) * PM + x_spec_slot<M>(kx),
-                rp.Sm + (fbase + fl) * fstride + (size_t)kx * plane + row_off + yy);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
-      const int l = it % (nloc * WY), pr = x_run_pair<M>(it / (nloc * WY));
-      x_inv_runs<M, SPEC_INPLACE>(lines + l * PM, 0, lines + l * PM, pr, sh.twN);
-    }
-  } else {
-    for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
-      const int l = it % (nloc * WY), pr = x_run_pair<M>(it / (nloc * WY));
-      const int fl = l / WY, yy = l - fl * WY;
-      x_inv_runs<M>(rp.Sm + (fbase + fl) * fstride + row_off + yy, plane, lines + l * PM, pr, sh.twN);
-    }
+  for (int it = threadIdx.x; it < nloc * WY * NP; it += T) {
+    const int l = it % (nloc * WY), pr = x_run_pair<M>(it / (nloc * WY));
+    const int fl = l / WY, yy = l - fl * WY;
+    x_inv_runs<M>(rp.Sm + (fbase + fl) * fstride + row_off + yy, plane, lines + l * PM, pr, sh.twN);
   }
   __syncthreads();
   passA_rt<M, PM, T, true>(lines, nloc * WY, sh.twM);

@@ -74,17 +74,15 @@ static int addlog(XKernels* out, int n) {
   return n;
 }
 
-// bulk pass split over two-CTA clusters (ASYNC: tiles copied in by cp.async);
-// the other modes use the one-CTA kernel
-template <int NX, int WY, int T, bool ASYNC = false>
+// bulk pass split over two-CTA clusters; the other modes use the one-CTA kernel
+template <int NX, int WY, int T>
 static int addcl(XKernels* out, int n) {
   if (n >= kMaxVariants) return n;
   n = add<NX, WY, T>(out, n);
   XKernels& k = out[n - 1];
-  k.bulk = x_pass_cl_kernel<NX, WY, T, ASYNC>;
+  k.bulk = x_pass_cl_kernel<NX, WY, T>;
   k.cl = 2;
   k.bulk_smem = cl_smem<NX, WY>;
-  k.tag = ASYNC ? ",async" : "";
   return n;
 }
 
@@ -113,8 +111,6 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = addlog<128, 8, 256>(out, n);
       n = addtma<128, 4, 256, 3>(out, n); n = addtma<128, 4, 384, 2>(out, n);
       n = addas<128, 8, 256>(out, n); n = addas<128, 8, 256, true>(out, n); n = addas<128, 4, 256>(out, n);
-      // fields split over two CTAs, tiles by cp.async: three CTAs (24 warps) per SM at 17 fields
-      n = addcl<128, 8, 256, true>(out, n);
       // many rows for the one-field xj pass (its bulk mode does not fit: never chosen for the bulk pass)
       n = add<128, 32, 256>(out, n);
       break;
@@ -124,10 +120,7 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = addtma<256, 4, 512>(out, n); n = addtma<256, 2, 512>(out, n);
       n = addas<256, 4, 512>(out, n); n = addas<256, 2, 256>(out, n);
       n = addcl<256, 8, 512>(out, n);  // fields split over two CTAs: 8-row (64-byte) tiles at 33 fields
-      // 24 warps in the one CTA an SM holds at 33 fields (runs of 8: at most 80 registers a thread)
-      n = add<256, 4, 768>(out, n); n = addas<256, 4, 768>(out, n);
       n = add<256, 1, 256>(out, n);  // one row per tile: up to 200 fields
-      n = addcl<256, 4, 256, true>(out, n);
       break;
     default: break;
   }
