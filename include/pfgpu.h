@@ -86,7 +86,7 @@ typedef struct pf_run pf_run;
  * 200, 256} (the reference's weak-scaling grids included; every
  * (Ny, Nz) pair with Ny == Nz plus the non-cubic pairs listed by
  * pf_supported_shape), 1 <= var <= 255 as long as var+1 field rows of the x
- * pass fit in shared memory (var <= 131 at Nx = 96, 98 at 128, 199 at 256).
+ * pass fit in shared memory (var <= 129 at Nx = 96, 97 at 128, 195 at 256).
  * The FP64 path takes any even Nx. */
 int pf_create(const pf_config* cfg, pf_run** out);
 

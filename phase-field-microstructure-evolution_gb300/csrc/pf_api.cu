@@ -150,6 +150,11 @@ static size_t x_smem(int nx, int nF, int wy) {
 
 static const size_t kMaxSmem = 227 * 1024;
 
+// Static shared memory of the one-CTA x-pass kernels beside the dynamic line
+// buffer: the twiddle tables (Nx + Nx/2 float2, from Nx = 96 up) and the
+// diagnostics reduction's arrays (under 1 KB).  Both count against kMaxSmem.
+static size_t x_static_smem(int nx) { return (nx >= 96 ? (size_t)(nx + nx / 2) * sizeof(float2) : 0) + 1024; }
+
 // cuTensorMapEncodeTiled through the runtime's driver entry points (no link
 // against the driver library).
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -198,7 +203,7 @@ static int validate(const pf_config* c) {
   if (c->var < 1 || c->var > kMaxVar) return fail(PF_EINVAL, "var=%d outside [1, %d]", c->var, kMaxVar);
   bool fits = false;
   for (int i = 0; i < nxv; ++i)
-    fits = fits || (c->ny % xv[i].wy == 0 && x_smem(c->nx, c->var + 1, xv[i].wy) <= kMaxSmem);
+    fits = fits || (c->ny % xv[i].wy == 0 && x_smem(c->nx, c->var + 1, xv[i].wy) + x_static_smem(c->nx) <= kMaxSmem);
   if (!fits) return fail(PF_EINVAL, "var=%d with Nx=%d, Ny=%d does not fit the x pass", c->var, c->nx, c->ny);
   if (c->mobility != PF_MOB_REFERENCE && c->mobility != PF_MOB_C1MC)
     return fail(PF_EINVAL, "unknown mobility form %d", c->mobility);
@@ -448,7 +453,7 @@ static bool raise_smem(const void* fn, size_t bytes) {
 static bool x_ok(pf_batch* b, const XKernels& k) {
   if (b->Ny % k.wy != 0) return false;
   const size_t sm = x_smem(b->Nx, b->nF, k.wy);
-  if (sm > kMaxSmem) return false;
+  if (sm + x_static_smem(b->Nx) > kMaxSmem) return false;
   if (k.tma) {  // persistent TMA bulk kernel: staging + lines must fit one CTA; inner TMA box of 16-byte multiples
     const size_t sb = k.bulk_smem(b->nF);
     CUtensorMap probe;
@@ -488,7 +493,7 @@ static bool x_ok(pf_batch* b, const XKernels& k) {
 static bool xj_ok(pf_batch* b, const XKernels& k) {
   if (b->Ny % k.wy != 0) return false;
   const size_t sm = x_smem(b->Nx, 1, k.wy);
-  return sm <= kMaxSmem && raise_smem((const void*)k.xj, sm);
+  return sm + x_static_smem(b->Nx) <= kMaxSmem && raise_smem((const void*)k.xj, sm);
 }
 
 static void describe_variants(pf_batch* b) {

@@ -212,10 +212,18 @@ struct XPlan<128> {
 template <int M>
 using XLine = Line<M, XPlan<M>::N1, XPlan<M>::N2>;
 
+// A twiddle of the x pass: from a copy of the table in shared memory (TWS),
+// else from the global table through the read-only path.
+template <bool TWS>
+__device__ __forceinline__ float2 ldtw(const float2* p) {
+  if constexpr (TWS) return *p;
+  else return __ldg(p);
+}
+
 // pass A over a runtime number of lines (pitch P, T threads).  A warp takes 32
 // consecutive lines at one column n1: with an odd pitch those 32 accesses hit
 // distinct bank pairs.
-template <int L, int P, int T, bool INV>
+template <int L, int P, int T, bool INV, bool TWS = false>
 __device__ __forceinline__ void passA_rt(float2* buf, int NL, const float2* __restrict__ tw) {
   constexpr int N1 = XLine<L>::N1, N2 = XLine<L>::N2;
   const int nlb = (NL + 31) >> 5;  // groups of 32 lines
@@ -231,11 +239,11 @@ __device__ __forceinline__ void passA_rt(float2* buf, int NL, const float2* __re
       for (int n2 = 0; n2 < N2; ++n2) v[n2] = p[n2 * (N1 + 1)];
       Dft<N2>::fwd(v);
 #pragma unroll
-      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], __ldg(tw + n1 * k2));
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], ldtw<TWS>(tw + n1 * k2));
     } else {
       v[0] = p[0];
 #pragma unroll
-      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * (N1 + 1)], __ldg(tw + n1 * k2));
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * (N1 + 1)], ldtw<TWS>(tw + n1 * k2));
       dft_inv<N2>(v);
     }
 #pragma unroll
@@ -279,7 +287,7 @@ __device__ __forceinline__ int x_run_pair(int q) {
 // Inverse x transform, first half: read the half spectrum of line (f, yy)
 // for the run pair `pr` (from where SRC says), pre-process, inverse DFT_N1 of
 // each run, store the runs (pass B' output) into the padded line.
-template <int M, int SRC = SPEC_GLOBAL>
+template <int M, int SRC = SPEC_GLOBAL, bool TWS = false>
 __device__ __forceinline__ void x_inv_runs(const float2* src, size_t plane, float2* line, int pr,
                                            const float2* __restrict__ twN) {  // src may be line (in place)
   constexpr int N1 = XLine<M>::N1, N2 = XLine<M>::N2;
@@ -295,7 +303,7 @@ __device__ __forceinline__ void x_inv_runs(const float2* src, size_t plane, floa
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) {
       const int k = ra + N2 * k1;
-      pre_pair(a[k1], b[N1 - 1 - k1], __ldg(twN + k), __ldg(twN + M - k), za[k1], zb[N1 - 1 - k1]);
+      pre_pair(a[k1], b[N1 - 1 - k1], ldtw<TWS>(twN + k), ldtw<TWS>(twN + M - k), za[k1], zb[N1 - 1 - k1]);
     }
     dft_inv<N1>(za);
     dft_inv<N1>(zb);
@@ -315,7 +323,7 @@ __device__ __forceinline__ void x_inv_runs(const float2* src, size_t plane, floa
     for (int k1 = 1; k1 <= N1 / 2; ++k1) {
       const int k = N2 * k1;
       float2 zk, zm;
-      pre_pair(a[k1], a[N1 - k1], __ldg(twN + k), __ldg(twN + M - k), zk, zm);
+      pre_pair(a[k1], a[N1 - k1], ldtw<TWS>(twN + k), ldtw<TWS>(twN + M - k), zk, zm);
       z[k1] = zk;
       if (k1 != N1 - k1) z[N1 - k1] = zm;
     }
@@ -331,7 +339,7 @@ __device__ __forceinline__ void x_inv_runs(const float2* src, size_t plane, floa
 #pragma unroll
     for (int k1 = 0; k1 < N1 / 2; ++k1) {
       const int k = ra + N2 * k1;
-      pre_pair(a[k1], a[N1 - 1 - k1], __ldg(twN + k), __ldg(twN + M - k), z[k1], z[N1 - 1 - k1]);
+      pre_pair(a[k1], a[N1 - 1 - k1], ldtw<TWS>(twN + k), ldtw<TWS>(twN + M - k), z[k1], z[N1 - 1 - k1]);
     }
     dft_inv<N1>(z);
 #pragma unroll
@@ -341,7 +349,7 @@ __device__ __forceinline__ void x_inv_runs(const float2* src, size_t plane, floa
 
 // Forward x transform, last half: forward DFT_N1 of the run pair `pr` (pass
 // B), post-process, store the half spectrum (scaled) to global.
-template <int M>
+template <int M, bool TWS = false>
 __device__ __forceinline__ void x_fwd_runs(float2* __restrict__ dst, size_t plane, const float2* line, int pr,
                                            float scale, const float2* __restrict__ twN) {
   constexpr int N1 = XLine<M>::N1, N2 = XLine<M>::N2;
@@ -360,7 +368,7 @@ __device__ __forceinline__ void x_fwd_runs(float2* __restrict__ dst, size_t plan
     for (int k1 = 0; k1 < N1; ++k1) {
       const int k = ra + N2 * k1;
       float2 xk, xm;
-      post_pair(za[k1], zb[N1 - 1 - k1], __ldg(twN + k), __ldg(twN + M - k), h, xk, xm);
+      post_pair(za[k1], zb[N1 - 1 - k1], ldtw<TWS>(twN + k), ldtw<TWS>(twN + M - k), h, xk, xm);
       dst[(size_t)k * plane] = xk;
       dst[(size_t)(M - k) * plane] = xm;
     }
@@ -375,7 +383,7 @@ __device__ __forceinline__ void x_fwd_runs(float2* __restrict__ dst, size_t plan
     for (int k1 = 1; k1 <= N1 / 2; ++k1) {
       const int k = N2 * k1;
       float2 xk, xm;
-      post_pair(z[k1], z[N1 - k1], __ldg(twN + k), __ldg(twN + M - k), h, xk, xm);
+      post_pair(z[k1], z[N1 - k1], ldtw<TWS>(twN + k), ldtw<TWS>(twN + M - k), h, xk, xm);
       dst[(size_t)k * plane] = xk;
       if (k1 != N1 - k1) dst[(size_t)(M - k) * plane] = xm;
     }
@@ -389,7 +397,7 @@ __device__ __forceinline__ void x_fwd_runs(float2* __restrict__ dst, size_t plan
     for (int k1 = 0; k1 < N1 / 2; ++k1) {
       const int k = ra + N2 * k1;
       float2 xk, xm;
-      post_pair(z[k1], z[N1 - 1 - k1], __ldg(twN + k), __ldg(twN + M - k), h, xk, xm);
+      post_pair(z[k1], z[N1 - 1 - k1], ldtw<TWS>(twN + k), ldtw<TWS>(twN + M - k), h, xk, xm);
       dst[(size_t)k * plane] = xk;
       dst[(size_t)(M - k) * plane] = xm;
     }
@@ -725,6 +733,21 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
   // run pairs (pr, N2 - pr) for 0 < pr < N2/2, run 0 alone, and for even N2
   // the run N2/2 paired with itself (x_inv_runs / x_fwd_runs)
   extern __shared__ float2 smem[];
+  // The twiddle tables W_NX^j and W_M^j, read by every run and pass-A item:
+  // copied to shared memory from Nx = 96 up.  There a CTA's tile of every
+  // field leaves room for one or two CTAs per SM, so the extra registers the
+  // compiler then spends on early twiddle loads cost no occupancy (x pass
+  // 0.129 -> 0.124 ms at 128^3 x 16, 2.67 -> 2.59 ms at 256^3 x 32); the
+  // small grids' tiles fit more CTAs than those registers would.
+  constexpr bool TWS = NX >= 96;
+  __shared__ float2 stwN[TWS ? NX : 1], stwM[TWS ? M : 1];
+  if constexpr (TWS) {
+    for (int j = threadIdx.x; j < NX; j += T) stwN[j] = __ldg(sh.twN + j);
+    for (int j = threadIdx.x; j < M; j += T) stwM[j] = __ldg(sh.twM + j);
+    __syncthreads();
+  }
+  const float2* twN = TWS ? stwN : sh.twN;
+  const float2* twM = TWS ? stwM : sh.twM;
   const RunParams& rp = runs[blockIdx.y];
   const int nF = (MODE == MODE_XJ) ? 1 : rp.V + 1;
   const int ny_tiles = sh.Ny / WY;
@@ -759,17 +782,17 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
       __syncthreads();
       for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
         const int l = it % (nF * WY), pr = x_run_pair<M>(it / (nF * WY));
-        x_inv_runs<M, SPEC_INPLACE>(smem + l * PM, 0, smem + l * PM, pr, sh.twN);
+        x_inv_runs<M, SPEC_INPLACE, TWS>(smem + l * PM, 0, smem + l * PM, pr, twN);
       }
     } else {
       for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
         const int l = it % (nF * WY), pr = x_run_pair<M>(it / (nF * WY));
         const int f = l / WY, yy = l - f * WY;
-        x_inv_runs<M>(src + f * fstride + row_off + yy, plane, smem + l * PM, pr, sh.twN);
+        x_inv_runs<M, SPEC_GLOBAL, TWS>(src + f * fstride + row_off + yy, plane, smem + l * PM, pr, twN);
       }
     }
     __syncthreads();
-    passA_rt<M, PM, T, true>(smem, nF * WY, sh.twM);
+    passA_rt<M, PM, T, true, TWS>(smem, nF * WY, twM);
   }
   __syncthreads();
 
@@ -803,14 +826,14 @@ __global__ void __launch_bounds__(T) x_pass_kernel(const RunParams* __restrict__
   }
 
   // 3. forward x transform: pass A, then pass B + post-processing -> global
-  passA_rt<M, PM, T, false>(smem, nF * WY, sh.twM);
+  passA_rt<M, PM, T, false, TWS>(smem, nF * WY, twM);
   __syncthreads();
   float2* __restrict__ dst = (MODE == MODE_BULK) ? rp.D : (MODE == MODE_XJ ? rp.J : rp.Sm);
   const float scale = 1.0f / (float)NX;
   for (int it = threadIdx.x; it < nF * WY * NP; it += T) {
     const int l = it % (nF * WY), pr = x_run_pair<M>(it / (nF * WY));
     const int f = l / WY, yy = l - f * WY;
-    x_fwd_runs<M>(dst + f * fstride + row_off + yy, plane, smem + l * PM, pr, scale, sh.twN);
+    x_fwd_runs<M, TWS>(dst + f * fstride + row_off + yy, plane, smem + l * PM, pr, scale, twN);
   }
 
   if (MODE != MODE_BULK) return;
@@ -1545,7 +1568,7 @@ struct YZ1 {
 };
 
 // column pass A (forward or inverse) over the NY y positions
-template <int NY, int NZ, int T, bool INV, bool RAWP>
+template <int NY, int NZ, int T, bool INV, bool RAWP, bool TWS = false>
 __device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
   constexpr int N1 = Line<NZ>::N1, N2 = Line<NZ>::N2, PY = YZ1<NY, NZ, RAWP>::PY;
   constexpr int ITEMS = NY * N1, ITER = (ITEMS + T - 1) / T;
@@ -1561,11 +1584,11 @@ __device__ __forceinline__ void colA(float2* U, const float2* __restrict__ tw) {
       for (int n2 = 0; n2 < N2; ++n2) v[n2] = p[n2 * N1 * PY];
       Dft<N2>::fwd(v);
 #pragma unroll
-      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], __ldg(tw + n1 * k2));
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmul(v[k2], ldtw<TWS>(tw + n1 * k2));
     } else {
       v[0] = p[0];
 #pragma unroll
-      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * N1 * PY], __ldg(tw + n1 * k2));
+      for (int k2 = 1; k2 < N2; ++k2) v[k2] = cmulc(p[k2 * N1 * PY], ldtw<TWS>(tw + n1 * k2));
       dft_inv<N2>(v);
     }
 #pragma unroll
@@ -1583,6 +1606,13 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   extern __shared__ float2 U[];
   __shared__ float4 qzt[NZ];  // kz factors of the k-space update
   stage_kz<NZ, T>(qzt, sh);   // read after the barriers of the forward passes
+  // the z twiddles of the column passes in shared memory from 128 x 128 planes
+  // up (one CTA per SM there: the registers of early loads cost no occupancy)
+  constexpr bool TWS = NY >= 128;
+  __shared__ float2 stwZ[TWS ? NZ : 1];
+  if constexpr (TWS)
+    for (int j = threadIdx.x; j < NZ; j += T) stwZ[j] = __ldg(sh.twZ + j);  // read after the first barrier
+  const float2* twZ = TWS ? stwZ : sh.twZ;
   const RunParams& rp = runs[blockIdx.y];
   const int p = sh.plane0 + (int)blockIdx.x;
   const int Kx = sh.Kx;
@@ -1623,7 +1653,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   __syncthreads();
   passB<NY, NZ, PY, T, false>(U);
   __syncthreads();
-  colA<NY, NZ, T, false, RAWP>(U, sh.twZ);
+  colA<NY, NZ, T, false, RAWP, TWS>(U, twZ);
   __syncthreads();
   // 2. last forward z pass, pointwise k-space update, first inverse z pass
   const KPlane P(rp, sh, kx, MODE, is_c, 1.0f / (float)(NY * NZ));
@@ -1669,7 +1699,7 @@ __global__ void __launch_bounds__(T) yz1_kernel(const RunParams* __restrict__ ru
   }
   if (MODE == YZ_IMPORT) return;
   __syncthreads();
-  colA<NY, NZ, T, true, RAWP>(U, sh.twZ);
+  colA<NY, NZ, T, true, RAWP, TWS>(U, twZ);
   __syncthreads();
   passB<NY, NZ, PY, T, true>(U);
   __syncthreads();

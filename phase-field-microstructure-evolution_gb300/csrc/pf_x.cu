@@ -120,7 +120,7 @@ int x_variants_a(int nx, XKernels* out, int n) {
       n = addtma<256, 4, 512>(out, n); n = addtma<256, 2, 512>(out, n);
       n = addas<256, 4, 512>(out, n); n = addas<256, 2, 256>(out, n);
       n = addcl<256, 8, 512>(out, n);  // fields split over two CTAs: 8-row (64-byte) tiles at 33 fields
-      n = add<256, 1, 256>(out, n);  // one row per tile: up to 200 fields
+      n = add<256, 1, 256>(out, n);  // one row per tile: up to 196 fields
       break;
     default: break;
   }

@@ -35,12 +35,13 @@ def test_supported_shapes(lib):
     assert lib.pf_supported_shape(96, 96, 96, 55, 32) == 1  # the reference's own grid and var
     assert lib.pf_supported_shape(48, 48, 48, 4, 32) == 0  # not a fused-path size
     assert lib.pf_supported_shape(48, 48, 48, 4, 64) == 1  # the FP64 path takes any even Nx
-    assert lib.pf_supported_shape(128, 128, 128, 98, 32) == 1
-    assert lib.pf_supported_shape(128, 128, 128, 99, 32) == 0  # x-pass rows no longer fit
-    assert lib.pf_supported_shape(96, 96, 96, 131, 32) == 1
-    assert lib.pf_supported_shape(96, 96, 96, 132, 32) == 0
-    assert lib.pf_supported_shape(256, 256, 256, 199, 32) == 1  # one-row tiles of 200 fields
-    assert lib.pf_supported_shape(256, 256, 256, 200, 32) == 0
+    # the x pass's tile of every field plus its static tables within 227 KB
+    assert lib.pf_supported_shape(128, 128, 128, 97, 32) == 1
+    assert lib.pf_supported_shape(128, 128, 128, 98, 32) == 0  # x-pass rows no longer fit
+    assert lib.pf_supported_shape(96, 96, 96, 129, 32) == 1
+    assert lib.pf_supported_shape(96, 96, 96, 130, 32) == 0
+    assert lib.pf_supported_shape(256, 256, 256, 195, 32) == 1  # one-row tiles of 196 fields
+    assert lib.pf_supported_shape(256, 256, 256, 196, 32) == 0
     assert lib.pf_supported_shape(64, 64, 64, 256, 32) == 0  # var limit
 
 
