@@ -591,6 +591,11 @@ static int tune_batch(pf_batch* b) {
       // in interleaved rounds, keeping the best time per variant: first the
       // x variants with the default yz variant, then the yz variants.
       const int ROUNDS = 3, REPS = 3;
+      // warm-up steps first, so that the first variants are not timed on a GPU
+      // still raising its clocks
+      for (int i = 0; i < 8; ++i)
+        if (enqueue_step(b, b->stream)) cudaGetLastError();
+      cudaStreamSynchronize(b->stream);
       auto time_steps = [&](float& out) {
         if (enqueue_step(b, b->stream)) { cudaGetLastError(); return; }
         cudaEventRecord(e0, b->stream);
