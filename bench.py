@@ -413,9 +413,9 @@ def run_ours(args):
     assert len(recs) == args.steps
 
     # x pass, yz pass (order-parameter planes and c planes as two launches on
-    # the graph's two branches), xj pass, yz C2 pass; the step's record is
-    # formed inside the yz pass
-    kernels_per_step = 5 if var_mob else 2
+    # the graph's two branches), xj pass, yz C2 pass, and the step's record
+    # kernel; with constant mobility x pass, yz pass and record
+    kernels_per_step = 6 if var_mob else 3
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "cell-steps/s x P", "n_gpus": ws, "steps": args.steps,
@@ -582,7 +582,7 @@ def run_ensemble(args):
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                          "what": "x + yz pass design bytes of all runs per batched step"},
             "runs_one_at_a_time": {"value": alone, "unit": METRIC, "runs": n1, "steps": k1},
-            "clocks": clk, "gpu_launches": 2 * args.steps, "kernel_variants": lib.pf_batch_variant(bh).decode()}
+            "clocks": clk, "gpu_launches": 3 * args.steps, "kernel_variants": lib.pf_batch_variant(bh).decode()}
     print(json.dumps(line), flush=True)
     b.close()
     return 0

@@ -120,6 +120,7 @@ static int build_tables(int Nx, int Ny, int Nz, DevTables& t) {
   s.Nx = Nx; s.Ny = Ny; s.Nz = Nz; s.Kx = Kx;
   s.plane0 = 0;
   s.pref_yz = 0;
+  s.par = 0;
   s.twM = (const float2*)(b + off_tw[0]);
   s.twN = (const float2*)(b + off_tw[1]);
   s.twY = (const float2*)(b + off_tw[2]);
@@ -241,10 +242,13 @@ struct pf_batch {
   double* dstage = nullptr;    // double staging for one run's AoS fields
   int ring = 0;
   cudaStream_t stream = nullptr;
-  cudaGraphExec_t gexec = nullptr;
+  cudaGraphExec_t gexec = nullptr;   // one step
+  cudaGraphExec_t gexec_k = nullptr; // kGraphSteps steps, each step's record beside the next step's x pass
   cudaStream_t side = nullptr;        // second branch of the captured step (concentration chain)
   cudaStream_t copy = nullptr;        // record copies of completed steps (never waits for later steps)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_c = nullptr;
+  cudaStream_t rec = nullptr;         // the step records of the multi-step graph
+  cudaEvent_t ev_yz = nullptr, ev_rec[2] = {nullptr, nullptr};
   int prio_hi = 0;                    // greatest stream priority of the device
   int nsm = 0;                        // multiprocessors of the device (persistent TMA x pass)
   int tma_occ = 1;                    // resident CTAs per SM of the chosen TMA x pass
@@ -381,6 +385,74 @@ static int enqueue_step(pf_batch* b, cudaStream_t s, bool branch = false) {
     if (rc) return rc;
   }
   return launch_record(b, s);
+}
+
+// Steps captured together in the multi-step graph.
+static constexpr int kGraphSteps = 4;
+
+// K steps for the multi-step graph.  Every step runs as in enqueue_step, but
+// its record goes to the record stream, where it runs beside the next step's
+// x pass instead of ahead of it.  Steps alternate the two sets of diagnostic
+// partials (Shape::par); a step waits for the record of the step two before
+// it, the last reader of its set.  The graph ends after its last record.
+static int enqueue_steps_overlapped(pf_batch* b, cudaStream_t s, int K, bool branch) {
+  const int R = b->nruns;
+  const bool var = b->mob != MOB_CONST;
+  const bool two = branch && var && b->side;
+  int rc = PF_OK;
+  for (int k = 0; k < K && rc == PF_OK; ++k) {
+    const int par = k & 1;
+    b->tab.sh.par = par;
+    if (k >= 2) PF_CUDA(cudaStreamWaitEvent(s, b->ev_rec[par], 0));
+    rc = launch_x_bulk(b, s);
+    if (rc) break;
+    if (two) {
+      const int pc = b->V * b->Kx;  // first plane of the c field
+      PF_CUDA(cudaEventRecord(b->ev_fork, s));
+      PF_CUDA(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
+      rc = launch_yz(b, b->yk.main, b->Kx, b->drp, R, b->side, pc, b->prio_hi);
+      if (rc) break;
+      PF_CUDA(cudaEventRecord(b->ev_c, b->side));
+      rc = launch_xj(b, b->side, b->prio_hi);
+      if (rc) break;
+      rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, b->side, 0, b->prio_hi);
+      if (rc) break;
+      PF_CUDA(cudaEventRecord(b->ev_join, b->side));
+      rc = launch_yz(b, b->yk.main, pc, b->drp, R, s);
+      if (rc) break;
+      PF_CUDA(cudaEventRecord(b->ev_yz, s));
+      PF_CUDA(cudaStreamWaitEvent(b->rec, b->ev_yz, 0));
+      PF_CUDA(cudaStreamWaitEvent(b->rec, b->ev_c, 0));
+      rc = launch_record(b, b->rec);
+      if (rc) break;
+      PF_CUDA(cudaEventRecord(b->ev_rec[par], b->rec));
+      PF_CUDA(cudaStreamWaitEvent(s, b->ev_join, 0));  // this step's c field before the next x pass
+    } else {
+      rc = launch_yz(b, b->yk.main, b->nF * b->Kx, b->drp, R, s);
+      if (rc) break;
+      PF_CUDA(cudaEventRecord(b->ev_yz, s));  // the record needs the yz partials only
+      PF_CUDA(cudaStreamWaitEvent(b->rec, b->ev_yz, 0));
+      rc = launch_record(b, b->rec);
+      if (rc) break;
+      PF_CUDA(cudaEventRecord(b->ev_rec[par], b->rec));
+      if (var) {
+        rc = launch_xj(b, s);
+        if (rc) break;
+        rc = launch_yz(b, b->yk.c2, b->Kx, b->drp, R, s);
+      }
+    }
+  }
+  b->tab.sh.par = 0;
+  if (rc) return rc;
+  PF_CUDA(cudaStreamWaitEvent(s, b->ev_rec[(K - 1) & 1], 0));
+  return PF_OK;
+}
+
+// n steps on the batch's stream: multi-step graphs, then single steps.
+static int launch_steps(pf_batch* b, int n) {
+  for (; b->gexec_k && n >= kGraphSteps; n -= kGraphSteps) PF_CUDA(cudaGraphLaunch(b->gexec_k, b->stream));
+  for (; n > 0; --n) PF_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+  return PF_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -686,6 +758,11 @@ static void destroy_batch(pf_batch* b) {
   if (!b) return;
   cudaSetDevice(b->device);
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->gexec_k) cudaGraphExecDestroy(b->gexec_k);
+  if (b->rec) cudaStreamDestroy(b->rec);
+  if (b->ev_yz) cudaEventDestroy(b->ev_yz);
+  for (cudaEvent_t ev : b->ev_rec)
+    if (ev) cudaEventDestroy(ev);
   if (b->stream) cudaStreamDestroy(b->stream);
   if (b->side) cudaStreamDestroy(b->side);
   if (b->copy) cudaStreamDestroy(b->copy);
@@ -744,7 +821,7 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   // partial arrays sized for every variant (at least one y row per x-pass
   // block, at most 16 CTAs per yz cluster)
   const size_t szPx = align((size_t)XD_COUNT * b->Nz * b->Ny * sizeof(double));
-  const size_t szPyz = align((size_t)16 * b->nF * b->Kx * sizeof(double));
+  const size_t szPyz = align((size_t)32 * b->nF * b->Kx * sizeof(double));  // 2 parities x 2 x clusters <= 16
   const size_t szDiag = align((size_t)b->ring * DR_COUNT * sizeof(double));
   const size_t szCnt = 256;   // step counter and error word (one 64-byte line each)
   const size_t szTmap = 256;  // TMA tensor map of Sm (128 bytes, 64-byte aligned)
@@ -810,6 +887,10 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_c, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&b->rec, cudaStreamNonBlocking, b->prio_hi);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_yz, cudaEventDisableTiming);
+  for (cudaEvent_t& ev : b->ev_rec)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "stream/events: %s", cudaGetErrorString(e)));
 
   rc = tune_batch(b);
@@ -824,6 +905,17 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   if (rc) { if (g) cudaGraphDestroy(g); return bail(rc); }
   if (e2 != cudaSuccess) return bail(fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2)));
   e = cudaGraphInstantiate(&b->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)));
+  // and kGraphSteps steps, the records beside the following steps
+  g = nullptr;
+  e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "begin capture: %s", cudaGetErrorString(e)));
+  rc = enqueue_steps_overlapped(b, b->stream, kGraphSteps, env_int("PFGPU_REDUCE_BRANCH", 1) != 0);
+  e2 = cudaStreamEndCapture(b->stream, &g);
+  if (rc) { if (g) cudaGraphDestroy(g); return bail(rc); }
+  if (e2 != cudaSuccess) return bail(fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2)));
+  e = cudaGraphInstantiate(&b->gexec_k, g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return bail(fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)));
   *out = b;
@@ -904,7 +996,8 @@ static int batch_step(pf_batch* b, int nsteps, pf_diag* diag) {
   int done = 0;
   while (done < nsteps) {
     const int chunk = std::min(nsteps - done, b->ring);
-    for (int s = 0; s < chunk; ++s) PF_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    const int rl = launch_steps(b, chunk);
+    if (rl) return rl;
     PF_CUDA(cudaStreamSynchronize(b->stream));
     b->hdiag.resize((size_t)b->ring * DR_COUNT);
     for (int r = 0; r < b->nruns; ++r) {
@@ -1021,7 +1114,8 @@ int pf_batch_destroy(pf_batch* b) {
 int pf_batch_enqueue(pf_batch* b, int nsteps) {
   if (!b) return fail(PF_EINVAL, "null batch");
   PF_CUDA(cudaSetDevice(b->device));
-  for (int s = 0; s < nsteps; ++s) PF_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+  const int rl = launch_steps(b, nsteps);
+  if (rl) return rl;
   for (int r = 0; r < b->nruns; ++r) b->steps_done[r] += nsteps;
   return PF_OK;
 }
@@ -1037,7 +1131,7 @@ size_t pf_batch_bytes(const pf_config* c, int nruns) {
   const bool var = c->mobility == PF_MOB_C1MC || c->D_gb != 0.0;
   auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const size_t per_run = 3 * align(nF * fieldc * 8) + (var ? align(ncell * 4) + align(fieldc * 8) : 0) +
-                         align((size_t)XD_COUNT * plane * 8) + align(16 * nF * Kx * 8) + align(1024 * DR_COUNT * 8) + 512;
+                         align((size_t)XD_COUNT * plane * 8) + align(32 * nF * Kx * 8) + align(1024 * DR_COUNT * 8) + 512;
   return per_run * nruns + nF * ncell * 12 + ((size_t)1 << 20);
 }
 // Steps run `run` has completed since its last set_fields (host count).

@@ -36,14 +36,17 @@ namespace cg = cooperative_groups;
 namespace pf {
 
 // Per-block diagnostic partials of the x pass (floats; the sums as
-// compensated hi + lo pairs): part_x[q * nblk_x + block].
+// compensated hi + lo pairs): part_x[(par * XQ_COUNT + q) * nblk_x + block],
+// par = Shape::par, the step's parity: the record of one step reads its
+// partials while the next step's x pass writes the other set.
 enum XDiag {
   XQ_FETA_H = 0, XQ_FETA_L, XQ_FCH_H, XQ_FCH_L, XQ_MASS_H, XQ_MASS_L,
   XQ_CMIN, XQ_CMAX, XQ_PHIMIN, XQ_PHIPMAX, XQ_BAD, XQ_COUNT
 };
-// room reserved per (z, y) row for the x partials (doubles' worth, any variant)
-constexpr int XD_COUNT = 8;
-static_assert(XQ_COUNT * 4 <= XD_COUNT * 8, "x partials must fit the reserved room");
+// room reserved per (z, y) row for the x partials of both parities (doubles'
+// worth, any variant)
+constexpr int XD_COUNT = 12;
+static_assert(2 * XQ_COUNT * 4 <= XD_COUNT * 8, "x partials must fit the reserved room");
 // Per-step diagnostic record layout (doubles)
 enum DiagRec {
   DR_STEP = 0, DR_FINT, DR_FETA, DR_FCH, DR_CMIN, DR_CMAX, DR_PHIMIN, DR_PHIPMAX, DR_MASS, DR_NONFINITE, DR_COUNT
@@ -59,8 +62,8 @@ struct RunParams {
   float2* D;       // [nF][Kx][Nz][Ny] x-spectra of dF/dphi_i and dF/dc
   float* mob;      // [Nz][Ny][Nx] mobility minus D_mean (variable mobility only)
   float2* J;       // [Kx][Nz][Ny] CH flux scratch (variable mobility only)
-  float* part_x;   // [XQ_COUNT][nblk_x]
-  float* part_yz;  // [2][nblk_yz]: hi and lo of each yz CTA's weighted f_int sum
+  float* part_x;   // [2][XQ_COUNT][nblk_x]: per step parity
+  float* part_yz;  // [2][2][nblk_yz]: per step parity, hi and lo of each yz CTA's weighted f_int sum
   double* diag;    // [ring][DR_COUNT]
   int* counter;    // step counter (device)
   unsigned* err;     // bit 0: a TMA tile of the x pass never arrived (the step's record is flagged)
@@ -90,6 +93,7 @@ struct Shape {
   // resident at once, so that CTA b fetches into L2 what CTA b + pref (which
   // starts about when b ends) will read; 0: none
   int pref_yz;
+  int par;  // parity of the step: which set of diagnostic partials its passes write and its record reads
 };
 
 // ---------------------------------------------------------------------------
@@ -566,7 +570,7 @@ __device__ __forceinline__ void bulk_slot(float2* smem, int yy, int slot, const 
 }
 
 // Block reduction of the x pass's diagnostics into the block's partials
-// part_x[q * nblk_x + blk] (all threads of the block call it).  Sums travel as
+// part_x[(par * XQ_COUNT + q) * nblk_x + blk] (all threads of the block call it).  Sums travel as
 // compensated FP32 pairs: FP64 arithmetic is scarce on this part, and a
 // serial FP64 chain at the end of every block held its shared memory (and
 // the next block) back.
@@ -598,7 +602,7 @@ __device__ __forceinline__ void store_block_diag(const BulkAcc& acc, const RunPa
     const int nn = __reduce_add_sync(0xffffffffu, in ? red_i[lane] : 0);
     if (lane == 0) {
       const int nbk = sh.nblk_x;
-      float* p = rp.part_x + blk;
+      float* p = rp.part_x + (size_t)sh.par * XQ_COUNT * nbk + blk;
       p[XQ_FETA_H * nbk] = a0.hi; p[XQ_FETA_L * nbk] = a0.lo;
       p[XQ_FCH_H * nbk] = a1.hi;  p[XQ_FCH_L * nbk] = a1.lo;
       p[XQ_MASS_H * nbk] = a2.hi; p[XQ_MASS_L * nbk] = a2.lo;
@@ -1085,7 +1089,7 @@ __global__ void __launch_bounds__(T) record_kernel(const RunParams* __restrict__
   const RunParams& rp = runs[blockIdx.x];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int nb = sh.nblk_x;
-  const float* __restrict__ px = rp.part_x;
+  const float* __restrict__ px = rp.part_x + (size_t)sh.par * XQ_COUNT * sh.nblk_x;
   FF eta = ff(0.f), ch = ff(0.f), mass = ff(0.f), fphi = ff(0.f), fc = ff(0.f);
   float cmin = 1.f, cmax = 0.f, pmin = 1.f, ppmax = 0.f;  // reference start values (:1076-1079)
   int bad = 0;
@@ -1101,8 +1105,9 @@ __global__ void __launch_bounds__(T) record_kernel(const RunParams* __restrict__
   }
   // f_int partials: the last nblk_yz / nF slots belong to the c planes
   const int nyz = sh.nblk_yz, cstart = nyz - nyz / (rp.V + 1);
+  const float* __restrict__ pyz = rp.part_yz + (size_t)sh.par * 2 * nyz;
   for (int i = t; i < nyz; i += T) {
-    const FF v = ff(__ldcg(rp.part_yz + i), __ldcg(rp.part_yz + nyz + i));
+    const FF v = ff(__ldcg(pyz + i), __ldcg(pyz + nyz + i));
     if (i < cstart) fphi.add(v);
     else fc.add(v);
   }
@@ -1172,8 +1177,9 @@ __device__ __forceinline__ void yz_finish(const RunParams& rp, const Shape& sh, 
   if (wid == 0) {
     const FF s = warp_sum_ff(lane < NW ? ff(red[0][lane], red[1][lane]) : ff(0.f));
     if (lane == 0) {
-      rp.part_yz[slot] = s.hi;
-      rp.part_yz[sh.nblk_yz + slot] = s.lo;
+      float* pyz = rp.part_yz + (size_t)sh.par * 2 * sh.nblk_yz;
+      pyz[slot] = s.hi;
+      pyz[sh.nblk_yz + slot] = s.lo;
     }
   }
 }
