@@ -777,6 +777,32 @@ static void destroy_batch(pf_batch* b) {
   delete b;
 }
 
+// Capture the one-step and the multi-step graphs on the batch's stream (again
+// after pf_batch_prioritize: kernel nodes keep the priority of the stream
+// they were captured on, and the graphs run with their nodes' priorities).
+static int capture_graphs(pf_batch* b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->gexec_k) cudaGraphExecDestroy(b->gexec_k);
+  b->gexec = b->gexec_k = nullptr;
+  const bool branch = env_int("PFGPU_REDUCE_BRANCH", 1) != 0;
+  for (int k : {1, kGraphSteps}) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail(PF_ECUDA, "begin capture: %s", cudaGetErrorString(e));
+    const int rc = k == 1 ? enqueue_step(b, b->stream, branch) : enqueue_steps_overlapped(b, b->stream, k, branch);
+    const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e2 != cudaSuccess) return fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2));
+    e = cudaGraphInstantiate(k == 1 ? &b->gexec : &b->gexec_k, g, cudaGraphInstantiateFlagUseNodePriority);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  }
+  return PF_OK;
+}
+
 static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   if (!out) return fail(PF_EINVAL, "null output pointer");
   *out = nullptr;
@@ -896,28 +922,8 @@ static int create_batch(const pf_config* cfgs, int nruns, pf_batch** out) {
   rc = tune_batch(b);
   if (rc) return bail(rc);
 
-  // capture one step as a CUDA graph
-  cudaGraph_t g = nullptr;
-  e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "begin capture: %s", cudaGetErrorString(e)));
-  rc = enqueue_step(b, b->stream, env_int("PFGPU_REDUCE_BRANCH", 1) != 0);
-  cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
-  if (rc) { if (g) cudaGraphDestroy(g); return bail(rc); }
-  if (e2 != cudaSuccess) return bail(fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2)));
-  e = cudaGraphInstantiate(&b->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
-  cudaGraphDestroy(g);
-  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)));
-  // and kGraphSteps steps, the records beside the following steps
-  g = nullptr;
-  e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "begin capture: %s", cudaGetErrorString(e)));
-  rc = enqueue_steps_overlapped(b, b->stream, kGraphSteps, env_int("PFGPU_REDUCE_BRANCH", 1) != 0);
-  e2 = cudaStreamEndCapture(b->stream, &g);
-  if (rc) { if (g) cudaGraphDestroy(g); return bail(rc); }
-  if (e2 != cudaSuccess) return bail(fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2)));
-  e = cudaGraphInstantiate(&b->gexec_k, g, cudaGraphInstantiateFlagUseNodePriority);
-  cudaGraphDestroy(g);
-  if (e != cudaSuccess) return bail(fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)));
+  rc = capture_graphs(b);
+  if (rc) return bail(rc);
   *out = b;
   return PF_OK;
 }
@@ -1185,7 +1191,7 @@ int pf_batch_prioritize(pf_batch* b) {
   PF_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, b->prio_hi));
   cudaStreamDestroy(b->stream);
   b->stream = s;
-  return PF_OK;
+  return capture_graphs(b);  // the main chain's nodes take the new stream's priority
 }
 // Number of compiled x-pass and yz-pass variants of a grid (the index range
 // of PFGPU_X_VARIANT / PFGPU_YZ_VARIANT).
