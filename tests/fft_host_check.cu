@@ -4,6 +4,7 @@
 // FP64 DFT, relative to the largest output magnitude:
 //   dft <R> <forward err> <inverse err>
 //   line <L> <forward err>
+//   xline <L> <forward err>   (the x pass's own factorization, where it differs)
 // The line transform runs pass A (DFT_N2 of the columns n1, twiddles
 // W_L^(n1 k2)) then pass B (DFT_N1 of the rows k2), exactly as the shared-
 // memory passes do, and reads frequency k at position pos_of_freq(k).
@@ -61,9 +62,11 @@ static void check_dft(std::mt19937& g) {
   printf("dft %d %.3e %.3e\n", R, rel_err(a, dft_ref(x, -1)), rel_err(b, dft_ref(x, +1)));
 }
 
-template <int L>
-static void check_line(std::mt19937& g) {
-  constexpr int N1 = Line<L>::N1, N2 = Line<L>::N2;
+// LN: the line type (its length, runs N1 and strides N2); tag: "line" for a
+// plan's factorization, "xline" for the x pass's own factorization.
+template <int L, class LN = Line<L>>
+static void check_line(std::mt19937& g, const char* tag = "line") {
+  constexpr int N1 = LN::N1, N2 = LN::N2;
   std::uniform_real_distribution<float> u(-1.f, 1.f);
   std::vector<float2> buf(L), tw(L);
   std::vector<cd> x(L);
@@ -88,10 +91,10 @@ static void check_line(std::mt19937& g) {
   }
   std::vector<cd> got(L);
   for (int k = 0; k < L; ++k) {
-    const float2 c = buf[Line<L>::pos_of_freq(k)];
+    const float2 c = buf[LN::pos_of_freq(k)];
     got[k] = cd(c.x, c.y);
   }
-  printf("line %d %.3e\n", L, rel_err(got, dft_ref(x, -1)));
+  printf("%s %d %.3e\n", tag, L, rel_err(got, dft_ref(x, -1)));
 }
 
 int main() {
@@ -102,5 +105,7 @@ int main() {
   check_line<32>(g); check_line<40>(g); check_line<48>(g); check_line<51>(g); check_line<64>(g); check_line<80>(g);
   check_line<96>(g); check_line<100>(g); check_line<102>(g); check_line<128>(g); check_line<160>(g); check_line<192>(g);
   check_line<200>(g); check_line<256>(g);
+  // the x pass's lines of 128 complex points (Nx = 256) as 8 x 16
+  check_line<128, Line<128, 8, 16>>(g, "xline");
   return 0;
 }

@@ -39,3 +39,10 @@ def test_register_dft_matches_fp64(fft_report, radix):
 def test_line_plan_matches_fp64(fft_report, length):
     (err,) = fft_report[("line", length)]
     assert err < TOL, (length, err)
+
+
+def test_x_pass_line_of_128_as_8_by_16(fft_report):
+    """The x pass factors its 128-point lines (Nx = 256) as 8 x 16, not as the
+    plan's 16 x 8."""
+    (err,) = fft_report[("xline", 128)]
+    assert err < TOL, err
