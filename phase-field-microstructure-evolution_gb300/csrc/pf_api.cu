@@ -780,26 +780,38 @@ static void destroy_batch(pf_batch* b) {
 // Capture the one-step and the multi-step graphs on the batch's stream (again
 // after pf_batch_prioritize: kernel nodes keep the priority of the stream
 // they were captured on, and the graphs run with their nodes' priorities).
+// The batch's graphs are replaced only when both captures succeed.
 static int capture_graphs(pf_batch* b) {
-  if (b->gexec) cudaGraphExecDestroy(b->gexec);
-  if (b->gexec_k) cudaGraphExecDestroy(b->gexec_k);
-  b->gexec = b->gexec_k = nullptr;
   const bool branch = env_int("PFGPU_REDUCE_BRANCH", 1) != 0;
-  for (int k : {1, kGraphSteps}) {
+  cudaGraphExec_t ex[2] = {nullptr, nullptr};
+  int rc = PF_OK;
+  for (int i = 0; i < 2 && rc == PF_OK; ++i) {
+    const int k = i == 0 ? 1 : kGraphSteps;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return fail(PF_ECUDA, "begin capture: %s", cudaGetErrorString(e));
-    const int rc = k == 1 ? enqueue_step(b, b->stream, branch) : enqueue_steps_overlapped(b, b->stream, k, branch);
-    const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
-    if (rc) {
-      if (g) cudaGraphDestroy(g);
-      return rc;
+    if (e != cudaSuccess) {
+      rc = fail(PF_ECUDA, "begin capture: %s", cudaGetErrorString(e));
+      break;
     }
-    if (e2 != cudaSuccess) return fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2));
-    e = cudaGraphInstantiate(k == 1 ? &b->gexec : &b->gexec_k, g, cudaGraphInstantiateFlagUseNodePriority);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    rc = k == 1 ? enqueue_step(b, b->stream, branch) : enqueue_steps_overlapped(b, b->stream, k, branch);
+    const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (rc == PF_OK && e2 != cudaSuccess) rc = fail(PF_ECUDA, "end capture: %s", cudaGetErrorString(e2));
+    if (rc == PF_OK) {
+      e = cudaGraphInstantiate(&ex[i], g, cudaGraphInstantiateFlagUseNodePriority);
+      if (e != cudaSuccess) rc = fail(PF_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    if (g) cudaGraphDestroy(g);
   }
+  if (rc != PF_OK) {
+    for (cudaGraphExec_t x : ex)
+      if (x) cudaGraphExecDestroy(x);
+    cudaGetLastError();
+    return rc;
+  }
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->gexec_k) cudaGraphExecDestroy(b->gexec_k);
+  b->gexec = ex[0];
+  b->gexec_k = ex[1];
   return PF_OK;
 }
 
@@ -1189,9 +1201,16 @@ int pf_batch_prioritize(pf_batch* b) {
   PF_CUDA(cudaStreamSynchronize(b->stream));
   cudaStream_t s = nullptr;
   PF_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, b->prio_hi));
-  cudaStreamDestroy(b->stream);
+  cudaStream_t old = b->stream;
   b->stream = s;
-  return capture_graphs(b);  // the main chain's nodes take the new stream's priority
+  const int rc = capture_graphs(b);  // the main chain's nodes take the new stream's priority
+  if (rc != PF_OK) {  // keep the batch as it was
+    b->stream = old;
+    cudaStreamDestroy(s);
+    return rc;
+  }
+  cudaStreamDestroy(old);
+  return PF_OK;
 }
 // Number of compiled x-pass and yz-pass variants of a grid (the index range
 // of PFGPU_X_VARIANT / PFGPU_YZ_VARIANT).
