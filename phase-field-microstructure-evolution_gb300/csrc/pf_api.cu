@@ -399,6 +399,10 @@ static int enqueue_steps_overlapped(pf_batch* b, cudaStream_t s, int K, bool bra
   const int R = b->nruns;
   const bool var = b->mob != MOB_CONST;
   const bool two = branch && var && b->side;
+  struct ParityReset {  // later launches outside the graph use the first set
+    Shape& sh;
+    ~ParityReset() { sh.par = 0; }
+  } reset{b->tab.sh};
   int rc = PF_OK;
   for (int k = 0; k < K && rc == PF_OK; ++k) {
     const int par = k & 1;
@@ -442,7 +446,6 @@ static int enqueue_steps_overlapped(pf_batch* b, cudaStream_t s, int K, bool bra
       }
     }
   }
-  b->tab.sh.par = 0;
   if (rc) return rc;
   PF_CUDA(cudaStreamWaitEvent(s, b->ev_rec[(K - 1) & 1], 0));
   return PF_OK;
