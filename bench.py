@@ -666,12 +666,18 @@ def run_serve(args):
         ids: "queue.Queue" = queue.Queue()
         done = {}
 
+        failed = []
+
         def waiter():  # collects results as they finish, beside the arrivals
             while True:
                 i = ids.get()
                 if i is None:
                     return
-                _, _, _, tm = pool.wait_aos(i)
+                try:
+                    _, _, _, tm = pool.wait_aos(i)
+                except Exception as exc:  # a failed request: report it after the stream
+                    failed.append((i, repr(exc)))
+                    continue
                 done[i] = (time.perf_counter(), tm)
 
         th = threading.Thread(target=waiter)
@@ -687,6 +693,9 @@ def run_serve(args):
             ids.put(rid)
         ids.put(None)
         th.join()
+        if failed:
+            pool.close()
+            raise RuntimeError(f"served requests failed at rate {rate}: {failed[:3]}")
         t_served = max(done[i][0] for i in order) - t0
         lat = [done[i][1]["total_s"] for i in order]
         ndev = pool.devices
